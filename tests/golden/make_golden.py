@@ -1,0 +1,245 @@
+"""Generate the golden fixtures in tests/golden/*.npz from the reference itself.
+
+Test infrastructure.  Runs the reference's UNMODIFIED Python source
+(``src/caustics`` of fbartolic/caustics) on the NumPy stand-in for JAX in
+``tests/golden/jaxshim``, with ``caustics.ehrlich_aberth_primitive.poly_roots``
+bound to the reference's own compiled C++ solver (``oracle/_ref/libref_ea.so``,
+built by ``make -C oracle ref`` from lib/ehrlich_aberth/ehrlich_aberth.h).
+
+Only the container that holds the reference checkout can run this script; the
+fixtures it writes are committed and are all that the tests read.
+
+Known deviations of this harness from the reference under real JAX:
+* random jitter (extended_source.py:79-98, :144-148) uses a NumPy generator,
+  not JAX's threefry stream;
+* roots come from the reference's C++ solver through ctypes instead of an XLA
+  custom call (identical code, compiled with g++ -O2 -DNDEBUG).
+
+Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import ctypes
+import os
+import subprocess
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def load_reference(ref_root):
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={ref_root}"])
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libref_ea.so"))
+    lib.ref_ea_solve.restype = ctypes.c_int
+    lib.ref_ea_solve.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3
+
+    sys.path.insert(0, os.path.join(HERE, "jaxshim"))
+    import jax.numpy as jnp  # the stand-in
+
+    def poly_roots(coeffs, itmax=2000, compensated=False, custom_init=False, roots_init=None):
+        # same contract as src/caustics/ehrlich_aberth_primitive.py:34-94
+        coeffs = np.asarray(coeffs, dtype=np.complex128)
+        ncoeffs = coeffs.shape[-1]
+        out_shape = coeffs.shape[:-1] + (ncoeffs - 1,)
+        flat = np.ascontiguousarray(coeffs.reshape(-1, ncoeffs)[:, ::-1])
+        size = flat.shape[0]
+        if custom_init:
+            init = np.ascontiguousarray(np.asarray(roots_init, dtype=np.complex128).reshape(size, ncoeffs - 1))
+        else:
+            init = np.zeros((size, ncoeffs - 1), dtype=np.complex128)
+        roots = np.zeros((size, ncoeffs - 1), dtype=np.complex128)
+        rc = lib.ref_ea_solve(size, ncoeffs - 1, int(itmax), int(bool(compensated)), int(bool(custom_init)),
+                              flat.ctypes.data, init.ctypes.data, roots.ctypes.data)
+        assert rc == 0
+        return jnp.asarray(roots.reshape(out_shape))
+
+    mod = types.ModuleType("caustics.ehrlich_aberth_primitive")
+    mod.poly_roots = poly_roots
+    sys.modules["caustics.ehrlich_aberth_primitive"] = mod
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import caustics  # noqa: F401
+    return lib, poly_roots
+
+
+def cfg1_points(n=10000):
+    # BASELINE workload "binary point source": x then y, each U[-1.5, 1.5], seed 0
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1.5, 1.5, n)
+    y = rng.uniform(-1.5, 1.5, n)
+    return x + 1j * y
+
+
+def cfg3_systems(nsys, npts, seed=1):
+    # BASELINE workload "triple point source": per-system s1,s2~U[.5,2], q1~logU[1e-4,1],
+    # q2~logU[1e-4,1e-1], psi~U[0,2pi]; positions U[-1.5,1.5]^2 (x then y)
+    rng = np.random.default_rng(seed)
+    s1 = rng.uniform(0.5, 2.0, nsys)
+    s2 = rng.uniform(0.5, 2.0, nsys)
+    q1 = 10 ** rng.uniform(-4, 0, nsys)
+    q2 = 10 ** rng.uniform(-4, -1, nsys)
+    psi = rng.uniform(0, 2 * np.pi, nsys)
+    x = rng.uniform(-1.5, 1.5, (nsys, npts))
+    y = rng.uniform(-1.5, 1.5, (nsys, npts))
+    return s1, s2, q1, q2, psi, x + 1j * y
+
+
+def near_caustic_points(caustic, rho, n, seed):
+    rng = np.random.default_rng(seed)
+    c = np.asarray(caustic).reshape(-1)
+    idx = rng.choice(len(c), size=n, replace=False)
+    phi = rng.uniform(-np.pi, np.pi, n)
+    r = rng.uniform(0.0, 2 * rho, n)
+    return c[idx] + r * np.exp(1j * phi)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    lib, poly_roots = load_reference(args.ref)
+    from caustics import point_source as ps
+    from caustics import extended_source as es
+    from caustics import lightcurve as lc
+    from caustics import multipole as mp
+    from caustics import utils as ut
+    out = {}
+    t0 = time.time()
+
+    # ---- coefficients (point_source.py:17-86, 89-1479) ----
+    rng = np.random.default_rng(11)
+    w = rng.uniform(-1.5, 1.5, 64) + 1j * rng.uniform(-1.5, 1.5, 64)
+    cb = np.stack([np.asarray(ps._poly_coeffs_binary(w, a, e1)) for a, e1 in [(0.45, 1 / 1.1), (0.55, 0.9), (1.2, 0.5)]])
+    out["coeffs_binary"] = dict(w=w, a=np.array([0.45, 0.55, 1.2]), e1=np.array([1 / 1.1, 0.9, 0.5]), coeffs=cb)
+    s1, s2, q1, q2, psi, wt = cfg3_systems(6, 16, seed=1)
+    ct = []
+    for k in range(6):
+        a, e1 = 0.5 * s1[k], q1[k] / (1 + q1[k] + q2[k])
+        e2, r3 = q1[k] * e1, s2[k] * np.exp(1j * psi[k])
+        ct.append(np.asarray(ps._poly_coeffs_triple(wt[k], a, r3, e1, e2)))
+    out["coeffs_triple"] = dict(s1=s1, s2=s2, q1=q1, q2=q2, psi=psi, w=wt, coeffs=np.stack(ct))
+
+    # ---- roots: cfg1 polynomials through the reference solver (ehrlich_aberth.h) ----
+    wc = cfg1_points()[:2000]
+    a, q = 0.45, 0.1
+    e1 = 1 / (1 + q)
+    xcm = a * (1 - q) / (1 + q)
+    coeffs = np.asarray(ps._poly_coeffs_binary(wc + xcm, a, e1))
+    out["roots_cfg1"] = dict(w=wc, coeffs=coeffs,
+                             roots_plain=np.asarray(poly_roots(coeffs, itmax=2500)),
+                             roots_comp=np.asarray(poly_roots(coeffs, itmax=2500, compensated=True)))
+    # the reference's own fixture (tests/test_ehrlich_aberth_primitive.py:19-27)
+    wf = np.linspace(0.3, 0.35, 10).astype(np.complex128)
+    cf = np.asarray(ps._poly_coeffs_binary(wf, 0.45, 0.8))
+    out["roots_fixture"] = dict(w=wf, coeffs=cf, roots_plain=np.asarray(poly_roots(cf)),
+                                roots_comp=np.asarray(poly_roots(cf, compensated=True)))
+
+    # ---- point-source magnification (point_source.py:1762-1830) ----
+    wfull = cfg1_points()
+    out["mag_ps_cfg1"] = dict(w=wfull, s=np.float64(0.9), q=np.float64(0.1),
+                              mag=np.asarray(ps.mag_point_source(wfull.copy(), nlenses=2, s=0.9, q=0.1)))
+    xg = np.linspace(-0.5, 0.5, 50)
+    wg = (xg[None, :] + 1j * xg[:, None]).reshape(-1)
+    out["mag_ps_grid"] = dict(w=wg, s=np.float64(0.9), q=np.float64(0.2),
+                              mag=np.asarray(ps.mag_point_source(wg.copy(), nlenses=2, s=0.9, q=0.2)))
+    s1, s2, q1, q2, psi, wt = cfg3_systems(8, 64, seed=1)
+    mt, zt, mk = [], [], []
+    for k in range(8):
+        mt.append(np.asarray(ps.mag_point_source(wt[k].copy(), nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k], psi=psi[k])))
+        a, e1 = 0.5 * s1[k], q1[k] / (1 + q1[k] + q2[k])
+        z, m = ps._images_point_source(wt[k] + a * (1 - q1[k]) / (1 + q1[k]), nlenses=3, a=a,
+                                       r3=s2[k] * np.exp(1j * psi[k]), e1=e1, e2=q1[k] * e1)
+        zt.append(np.asarray(z)); mk.append(np.asarray(m))
+    out["mag_ps_triple"] = dict(s1=s1, s2=s2, q1=q1, q2=q2, psi=psi, w=wt, mag=np.stack(mt),
+                                z=np.stack(zt), mask=np.stack(mk))
+    print(f"[golden] point source done {time.time() - t0:.1f}s", flush=True)
+
+    # ---- critical curves and caustics (point_source.py:1582-1649) ----
+    zcr, zca = ps.critical_and_caustic_curves(npts=50, nlenses=2, s=0.9, q=0.2)
+    out["caustics_binary"] = dict(s=np.float64(0.9), q=np.float64(0.2), npts=np.int64(50),
+                                  z_cr=np.asarray(zcr), z_ca=np.asarray(zca))
+
+    # ---- hexadecapole + proximity tests (multipole.py, lightcurve.py:23-85) ----
+    hx = {}
+    for tag, (s, q, rho) in {"q0.2": (0.9, 0.2, 1e-2), "q5e-3": (1.1, 5e-3, 1e-2), "q0.05": (1.3, 0.05, 3e-3)}.items():
+        a, e1 = 0.5 * s, 1 / (1 + q)
+        xcm = a * (1 - q) / (1 + q)
+        _, cau = ps.critical_and_caustic_curves(npts=60, nlenses=2, s=s, q=q)
+        wpts = np.concatenate([near_caustic_points(cau, 10 * rho, 80, seed=5),
+                               np.random.default_rng(6).uniform(-1, 1, 40) + 1j * np.random.default_rng(7).uniform(-1, 1, 40)])
+        z, m = ps._images_point_source(wpts + xcm, nlenses=2, a=a, e1=e1)
+        mu, dmu = mp._mag_hexadecapole(z, m, rho, nlenses=2, a=a, e1=e1)
+        t1 = lc._caustics_proximity_test(wpts + xcm, z, m, rho, dmu, nlenses=2, a=a, e1=e1)
+        t2 = lc._planetary_caustic_test(wpts + xcm, rho, a=a, e1=e1)
+        hx[tag] = dict(s=np.float64(s), q=np.float64(q), rho=np.float64(rho), w=wpts, z=np.asarray(z),
+                       mask=np.asarray(m), mu_multi=np.asarray(mu), delta_mu=np.asarray(dmu),
+                       test_prox=np.asarray(t1), test_planet=np.asarray(t2))
+    for tag, d in hx.items():
+        out["hex_" + tag] = d
+    print(f"[golden] hexadecapole done {time.time() - t0:.1f}s", flush=True)
+
+    # ---- KAT-style helpers (utils.py, extended_source.py:156-216) ----
+    z = np.array([0.0, 1.0, 1.01, 1.02, 1.03, 0.0, 4.0, 4.01, 0.0, 0.0, 6.0]).astype(np.complex128)
+    par = np.array([-1., -1., -1., 1., 1., 1., 1., 1., 1., 1., 1.])
+    msk = np.array([0., 1., 1., 1., 1., 0., 1., 1., 0., 0., 1.])
+    out["split_segment"] = dict(z=z, parity=par, mask=msk,
+                                parts=np.asarray(es._split_segment(np.stack([z, par, msk]), n_parts=5)))
+
+    # ---- limb images (extended_source.py:56-153) ----
+    limb = {}
+    for k, (w0, rho, npts) in enumerate([(0.1 + 0.05j, 0.05, 100), (-0.3 + 0.02j, 1e-2, 200), (0.35 + 0.0j, 0.1, 60)]):
+        a, e1 = 0.45, 1 / 1.2
+        zl, ml, pl = es._images_of_source_limb(w0 + a * (1 - 0.2) / 1.2, rho, nlenses=2, npts=npts, a=a, e1=e1)
+        limb[f"limb{k}"] = dict(w0=np.complex128(w0), rho=np.float64(rho), npts=np.int64(npts), s=np.float64(0.9),
+                                q=np.float64(0.2), z=np.asarray(zl), mask=np.asarray(ml), parity=np.asarray(pl))
+    out.update(limb)
+
+    # ---- extended source magnification (extended_source.py:741-904) ----
+    _, cau = ps.critical_and_caustic_curves(npts=50, nlenses=2, s=0.9, q=0.2)
+    cases = []
+    for rho, npts_limb, ld, u1, seed in [(1e-1, 200, False, 0.0, 21), (1e-2, 300, False, 0.0, 22), (1e-3, 200, False, 0.0, 23),
+                                         (1e-1, 200, True, 0.7, 24), (1e-2, 300, True, 0.7, 25), (5e-2, 100, True, 0.3, 26)]:
+        wpts = np.concatenate([near_caustic_points(cau, rho, 5, seed), [0.6 + 0.4j]])
+        mags = np.array([float(es.mag_extended_source(wv, rho, nlenses=2, npts_limb=npts_limb, limb_darkening=ld,
+                                                         u1=u1, npts_ld=100, s=0.9, q=0.2)) for wv in wpts])
+        cases.append(dict(w=wpts, rho=np.float64(rho), npts_limb=np.int64(npts_limb), ld=np.bool_(ld), u1=np.float64(u1),
+                          s=np.float64(0.9), q=np.float64(0.2), mag=mags))
+        print(f"[golden] mag_es rho={rho} ld={ld} {time.time() - t0:.1f}s", flush=True)
+    for k, c in enumerate(cases):
+        out[f"mag_es{k}"] = c
+
+    # ---- light curve (lightcurve.py:99-254): the cfg2 trajectory, every 100th point, and a q>0.01 curve ----
+    t = np.linspace(-40.0, 40.0, 2000)
+    tau = t / 20.0
+    u0, alpha = 0.05, 0.6
+    wtraj = (u0 * np.cos(alpha) + tau * np.sin(alpha)) + 1j * (-u0 * np.sin(alpha) + tau * np.cos(alpha))
+    sub = wtraj[::100]
+    mags = np.asarray(lc.mag(sub, 1e-2, nlenses=2, npts_limb=500, limb_darkening=True, u1=0.5, npts_ld=100, s=1.1, q=5e-3))
+    out["mag_lc_cfg2"] = dict(w=sub, rho=np.float64(1e-2), u1=np.float64(0.5), s=np.float64(1.1), q=np.float64(5e-3),
+                              npts_limb=np.int64(500), npts_ld=np.int64(100), mag=mags)
+    print(f"[golden] mag cfg2 {time.time() - t0:.1f}s", flush=True)
+    wq = np.linspace(-0.8, 0.8, 24) + 0.08j
+    mags = np.asarray(lc.mag(wq, 2e-2, nlenses=2, npts_limb=200, limb_darkening=True, u1=0.4, npts_ld=60, s=0.95, q=0.3))
+    out["mag_lc_q0.3"] = dict(w=wq, rho=np.float64(2e-2), u1=np.float64(0.4), s=np.float64(0.95), q=np.float64(0.3),
+                              npts_limb=np.int64(200), npts_ld=np.int64(60), mag=mags)
+    print(f"[golden] mag q0.3 {time.time() - t0:.1f}s", flush=True)
+
+    # ---- triple extended source (nlenses=3) ----
+    s, q, q3, r3, psi = 1.0, 0.5, 0.05, 0.9, 1.1
+    wpts = np.array([0.02 + 0.03j, -0.15 + 0.1j, 0.4 - 0.25j])
+    mags = np.array([float(es.mag_extended_source(wv, 2e-2, nlenses=3, npts_limb=200, s=s, q=q, q3=q3, r3=r3, psi=psi))
+                     for wv in wpts])
+    out["mag_es_triple"] = dict(w=wpts, rho=np.float64(2e-2), npts_limb=np.int64(200), s=np.float64(s), q=np.float64(q),
+                                q3=np.float64(q3), r3=np.float64(r3), psi=np.float64(psi), mag=mags)
+    print(f"[golden] triple {time.time() - t0:.1f}s", flush=True)
+
+    for name, d in out.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print(f"[golden] wrote {len(out)} fixtures in {time.time() - t0:.1f}s")
+
+
+if __name__ == "__main__":
+    main()
