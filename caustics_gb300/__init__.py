@@ -1,0 +1,17 @@
+"""caustics_gb300: GB300-native (sm_103a) magnification hot path of
+fbartolic/caustics — Ehrlich-Aberth root solver, point-source and
+extended-source (contour-integration) magnification, hexadecapole routing —
+behind a C ABI (include/caustics_gb300.h) with the reference's Python
+signatures."""
+from .api import (  # noqa: F401
+    ehrlich_aberth,
+    lens_eq,
+    lens_eq_det_jac,
+    mag,
+    mag_extended_source,
+    mag_point_source,
+    poly_roots,
+)
+
+__all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
+           "mag"]

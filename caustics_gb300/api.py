@@ -1,0 +1,227 @@
+"""Drop-in magnification API with the reference's signatures, on CUDA tensors.
+
+Signature parity with fbartolic/caustics:
+  poly_roots / ehrlich_aberth ... src/caustics/ehrlich_aberth_primitive.py:34-106
+  mag_point_source .............. src/caustics/point_source.py:1763
+  mag_extended_source ........... src/caustics/extended_source.py:741-752
+  mag ........................... src/caustics/lightcurve.py:99-110
+  lens_eq, lens_eq_det_jac ...... src/caustics/point_source.py:1536-1580
+
+Inputs may be torch tensors (any device; CUDA tensors stay on their device)
+or array-likes (copied to the current CUDA device; NumPy out).  Every
+computation runs in libcaustics_gb300 on the current torch CUDA stream.
+Extra keyword ``precision`` selects "fp64" (the reference's arithmetic,
+default) or "mixed" (FP32 iterations with FP64 polish / accumulation).
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+_PREC = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED, "fp64_comp": L.PREC_FP64_COMP}
+
+
+def _stream():
+    return ctypes_void(torch.cuda.current_stream().cuda_stream)
+
+
+def ctypes_void(x):
+    import ctypes
+    return ctypes.c_void_p(int(x))
+
+
+def _ptr(t):
+    import ctypes
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+def _to_device(x, dtype):
+    was_numpy = not isinstance(x, torch.Tensor)
+    if was_numpy:
+        if not torch.cuda.is_available():
+            raise L.CausticsError("caustics_gb300 needs a CUDA device (no CPU fallback)")
+        t = torch.as_tensor(np.asarray(x), dtype=dtype).cuda()
+    else:
+        if not x.is_cuda:
+            if not torch.cuda.is_available():
+                raise L.CausticsError("caustics_gb300 needs a CUDA device (no CPU fallback)")
+            x = x.cuda()
+        t = x.to(dtype)
+    return t.contiguous(), was_numpy
+
+
+def _out(t, was_numpy):
+    return t.cpu().numpy() if was_numpy else t
+
+
+def _precision(p):
+    if p not in _PREC:
+        raise ValueError(f"precision must be one of {sorted(_PREC)}")
+    return _PREC[p]
+
+
+# ---------------------------------------------------------------------------
+# root solver primitive
+# ---------------------------------------------------------------------------
+
+def ehrlich_aberth(coeffs, roots_init, itmax=None, compensated=None, custom_init=False, precision=None, status=None):
+    """Batched primitive: coeffs complex128 [M, deg+1] low->high, roots_init
+    [M, deg]; returns roots [M*deg] (ehrlich_aberth_primitive.py:98-106)."""
+    c, was_np = _to_device(coeffs, torch.complex128)
+    m, n1 = c.shape
+    deg = n1 - 1
+    roots = torch.empty((m, deg), dtype=torch.complex128, device=c.device)
+    ri = None
+    if custom_init:
+        ri, _ = _to_device(roots_init, torch.complex128)
+        ri = ri.reshape(m, deg).contiguous()
+    prec = _precision(precision) if precision else (L.PREC_FP64_COMP if compensated else L.PREC_FP64)
+    st = status if status is not None else None
+    with torch.cuda.device(c.device):
+        L.check(L.lib().cgb_ea_solve(_ptr(c), _ptr(ri), _ptr(roots), m, deg, int(itmax or 2000), prec, _ptr(st),
+                                     _stream()), "cgb_ea_solve")
+    return _out(roots.reshape(-1), was_np)
+
+
+def poly_roots(coeffs, itmax=2000, compensated=False, custom_init=False, roots_init=None, precision=None):
+    """Roots of complex polynomials whose last axis holds the coefficients,
+    highest order first (ehrlich_aberth_primitive.py:34-94)."""
+    c, was_np = _to_device(coeffs, torch.complex128)
+    ncoeffs = c.shape[-1]
+    out_shape = tuple(c.shape[:-1]) + (ncoeffs - 1,)
+    flat = c.reshape(-1, ncoeffs).flip(-1).contiguous()
+    r = ehrlich_aberth(flat, roots_init, itmax=itmax, compensated=compensated, custom_init=custom_init,
+                       precision=precision)
+    return _out(r.reshape(out_shape), was_np)
+
+
+# ---------------------------------------------------------------------------
+# lens equation helpers (elementwise, on device)
+# ---------------------------------------------------------------------------
+
+def _lens_geometry(nlenses, params):
+    if nlenses == 1:
+        return [0.0 + 0.0j], [1.0], 0.0
+    if nlenses == 2:
+        if "a" in params:
+            a, e1 = params["a"], params["e1"]
+            return [a, -a], [e1, 1.0 - e1], 0.0
+        s, q = params["s"], params["q"]
+        a = 0.5 * s
+        e1 = 1.0 / (1.0 + q)
+        return [a, -a], [e1, 1.0 - e1], a * (1 - q) / (1 + q)
+    if nlenses == 3:
+        if "a" in params:
+            a, r3, e1, e2 = params["a"], params["r3"], params["e1"], params["e2"]
+            return [a, -a, complex(r3)], [e1, e2, 1.0 - e1 - e2], 0.0
+        s, q, q3, r3, psi = (params[k] for k in ("s", "q", "q3", "r3", "psi"))
+        a = 0.5 * s
+        e1 = q / (1.0 + q + q3)
+        e2 = q * e1
+        return [a, -a, r3 * complex(math.cos(psi), math.sin(psi))], [e1, e2, 1.0 - e1 - e2], a * (1 - q) / (1 + q)
+    raise ValueError("`nlenses` has to be set to be <= 3.")
+
+
+def lens_eq(z, nlenses=2, **params):
+    """w = z - sum_j eps_j / (conj(z) - conj(r_j)) with the reference's
+    (a, e1[, e2, r3]) parameters (point_source.py:1536-1556)."""
+    zt, was_np = _to_device(z, torch.complex128)
+    r, eps, _ = _lens_geometry(nlenses, params)
+    zb = torch.conj(zt)
+    w = zt.clone()
+    for rj, ej in zip(r, eps):
+        w = w - ej / (zb - complex(rj).conjugate())
+    return _out(w, was_np)
+
+
+def lens_eq_det_jac(z, nlenses=2, **params):
+    """point_source.py:1558-1580."""
+    zt, was_np = _to_device(z, torch.complex128)
+    r, eps, _ = _lens_geometry(nlenses, params)
+    zb = torch.conj(zt)
+    s = torch.zeros_like(zt)
+    for rj, ej in zip(r, eps):
+        s = s + ej / (zb - complex(rj).conjugate()) ** 2
+    return _out(1.0 - torch.abs(s) ** 2, was_np)
+
+
+# ---------------------------------------------------------------------------
+# magnifications
+# ---------------------------------------------------------------------------
+
+def mag_point_source(w, nlenses=2, roots_itmax=2500, roots_compensated=False, precision=None, return_status=False,
+                     return_images=False, **params):
+    """Point-source magnification (point_source.py:1762-1830)."""
+    wt, was_np = _to_device(w, torch.complex128)
+    shape = wt.shape
+    wf = wt.reshape(-1).contiguous()
+    n = wf.numel()
+    mag = torch.empty(n, dtype=torch.float64, device=wf.device)
+    st = torch.zeros(n, dtype=torch.int32, device=wf.device)
+    deg = nlenses * nlenses + 1
+    imgs = torch.empty((n, deg), dtype=torch.complex128, device=wf.device) if return_images else None
+    msk = torch.empty(n, dtype=torch.int32, device=wf.device) if return_images else None
+    prec = _precision(precision) if precision else (L.PREC_FP64_COMP if roots_compensated else L.PREC_FP64)
+    with torch.cuda.device(wf.device):
+        L.check(L.lib().cgb_mag_point_source(_ptr(wf), _ptr(mag), _ptr(imgs), _ptr(msk), n,
+                                             L.lens_params(nlenses, params), int(roots_itmax), prec, _ptr(st),
+                                             _stream()), "cgb_mag_point_source")
+    out = [_out(mag.reshape(shape), was_np)]
+    if return_images:
+        out += [_out(imgs.reshape(tuple(shape) + (deg,)), was_np), _out(msk.reshape(shape), was_np)]
+    if return_status:
+        out.append(_out(st.reshape(shape), was_np))
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0):
+    return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
+                       _precision(precision or "fp64"), int(grid))
+
+
+def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
+                        roots_itmax=2500, roots_compensated=False, precision=None, return_status=False, grid=0,
+                        **params):
+    """Extended-source magnification (extended_source.py:741-904).  w0 may be a
+    scalar (as in the reference) or an array of source centres (batched)."""
+    scalar = np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor)
+    wt, was_np = _to_device(np.atleast_1d(w0) if scalar else w0, torch.complex128)
+    shape = wt.shape
+    wf = wt.reshape(-1).contiguous()
+    n = wf.numel()
+    mag = torch.empty(n, dtype=torch.float64, device=wf.device)
+    st = torch.zeros(n, dtype=torch.int32, device=wf.device)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    with torch.cuda.device(wf.device):
+        L.check(L.lib().cgb_mag_extended_source(_ptr(wf), _ptr(mag), n, float(rho), L.lens_params(nlenses, params),
+                                                opts, _ptr(st), _stream()), "cgb_mag_extended_source")
+    if scalar:
+        m = float(mag[0].item())
+        return (m, int(st[0].item())) if return_status else m
+    out = _out(mag.reshape(shape), was_np)
+    return (out, _out(st.reshape(shape), was_np)) if return_status else out
+
+
+def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, npts_ld=100, roots_itmax=2500,
+        roots_compensated=False, precision=None, return_route=False, return_status=False, grid=0, **params):
+    """Light curve: hexadecapole where the reference's tests accept it, contour
+    integration elsewhere (lightcurve.py:99-254)."""
+    wt, was_np = _to_device(w_points, torch.complex128)
+    shape = wt.shape
+    wf = wt.reshape(-1).contiguous()
+    n = wf.numel()
+    out = torch.empty(n, dtype=torch.float64, device=wf.device)
+    route = torch.empty(n, dtype=torch.uint8, device=wf.device)
+    st = torch.zeros(n, dtype=torch.int32, device=wf.device)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    with torch.cuda.device(wf.device):
+        L.check(L.lib().cgb_mag(_ptr(wf), _ptr(out), _ptr(route), n, float(rho), L.lens_params(nlenses, params), opts,
+                                _ptr(st), _stream()), "cgb_mag")
+    res = [_out(out.reshape(shape), was_np)]
+    if return_route:
+        res.append(_out(route.reshape(shape).bool(), was_np))
+    if return_status:
+        res.append(_out(st.reshape(shape), was_np))
+    return res[0] if len(res) == 1 else tuple(res)

@@ -1,0 +1,339 @@
+// Ehrlich-Aberth simultaneous root solvers, one polynomial per thread, roots in
+// registers (DEG is a compile-time constant so every array index is static).
+//
+// aberth64      FP64, the reference's iteration (lib/ehrlich_aberth/ehrlich_aberth.h:60-150):
+//               Gauss-Seidel updates, reversed polynomial in 1/z when |z| > 1,
+//               stop a root when |p(z)| <= EPS * sum |a_i| (1 + 3.828 i) |z|^i.
+// aberth64_comp adds the reference's compensated second stage
+//               (ehrlich_aberth.h:153-292) with an FP64 error-free Horner.
+// aberth_mixed  FP32 iteration, then a compensated Horner stage in FP32 with
+//               double-float coefficients (TwoSum / TwoProd via FMA) that drives
+//               every root to float resolution against the FP64 polynomial, then
+//               FP64 Newton polish; a root set that is not resolved falls back to
+//               aberth64 from the polished roots.
+//
+// Initial estimates follow init_est.h:37-102 (radii from the upper convex hull
+// of (i, log|a_i|)) but are complex: r*exp(i*phi).  The reference's guesses are
+// real, r*sin(phi) (init_est.h:95), which only converge for real-coefficient
+// polynomials through the rounding of thrust::pow.
+#pragma once
+#include "cplx.cuh"
+
+#define CGB_EPS64 1.1102230246251565e-16
+#define CGB_EPS32 5.9604644775390625e-08f
+
+// per-item status bits (also exported in include/caustics_gb300.h)
+#define CGB_ST_NOCONV 1u     // root solver reached itmax
+#define CGB_ST_AMBIGUOUS 2u  // a lens-equation residual within x30 of the 1e-6 image threshold
+#define CGB_ST_FALLBACK 4u   // mixed solver fell back to FP64 Aberth
+#define CGB_ST_MERGE 8u      // contour linking left open segments or overflowed its buffer
+#define CGB_ST_CAPACITY 16u  // limb / contour buffers too small for the request
+
+template <int DEG, typename R>
+__device__ __forceinline__ void init_estimates(const R (&alpha)[DEG + 1], cd (&z)[DEG]) {
+  double hx[DEG + 1], hy[DEG + 1], al[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) al[i] = (double)alpha[i];
+  int k = 0;
+  for (int i = DEG; i >= 0; --i) {
+    double y = al[i] > 0 ? log(al[i]) : -1e30;
+    while (k >= 2 && (hx[k - 1] - hx[k - 2]) * (y - hy[k - 2]) - (hy[k - 1] - hy[k - 2]) * ((double)i - hx[k - 2]) <= 0)
+      --k;
+    hx[k] = i;
+    hy[k] = y;
+    ++k;
+  }
+  cd t[DEG];
+  const double pi2 = 6.28318530717958647693, th = pi2 / DEG;
+  int n = 0;
+  for (int i = k - 2; i >= 0; --i) {
+    int nz = (int)(hx[i] - hx[i + 1]);
+    double r = exp((hy[i + 1] - hy[i]) / nz);
+    if (!(r > 0.0) || !isfinite(r)) r = 1.0;
+    double ang = pi2 / nz;
+    for (int j = 0; j < nz && n + j < DEG; ++j) {
+      double s, c;
+      sincos(ang * j + th * i + 0.7, &s, &c);
+      t[n + j] = mk(r * c, r * s);
+    }
+    n += nz;
+  }
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) z[i] = t[i];
+}
+
+// sum_{i != j} 1 / (z_j - z_i)
+template <int DEG, typename C>
+__device__ __forceinline__ C aberth_sum(const C (&z)[DEG], int j) {
+  C s = z[0] - z[0];
+#pragma unroll
+  for (int i = 0; i < DEG; ++i)
+    if (i != j) s = s + crecip(z[j] - z[i]);
+  return s;
+}
+
+// Horner for p and p' at x; rev walks the coefficients from p[0] (the reversed
+// polynomial evaluated at x = 1/z).  b = the real bound polynomial at |x|.
+template <int DEG, typename C, typename R>
+__device__ __forceinline__ void horner_pair(const C (&p)[DEG + 1], const R (&alpha)[DEG + 1], C x, R ax, bool rev,
+                                            C &h, C &hd, R &b) {
+  h = rev ? p[0] : p[DEG];
+  b = rev ? alpha[0] : alpha[DEG];
+  hd = h - h;
+#pragma unroll
+  for (int k = 1; k <= DEG; ++k) {
+    C pk = rev ? p[k] : p[DEG - k];
+    R ak = rev ? alpha[k] : alpha[DEG - k];
+    hd = cfma(hd, x, h);
+    h = cfma(h, x, pk);
+    b = b * ax + ak;
+  }
+}
+
+// Aberth correction; rev form from ehrlich_aberth.h:43-58
+template <int DEG, typename C>
+__device__ __forceinline__ C aberth_corr(const C (&z)[DEG], int j, C h, C hd, bool rev) {
+  C s = aberth_sum<DEG, C>(z, j);
+  if (rev) {
+    C z2h = z[j] * z[j] * h;
+    C d = z[j] * h;
+    d = C{d.x * DEG, d.y * DEG} - hd - z2h * s;
+    return cdiv(z2h, d);
+  }
+  return cdiv(h, hd - h * s);
+}
+
+template <int DEG>
+__device__ int aberth64(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
+  double alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = cabs(p[i]);
+  if (!warm) init_estimates<DEG>(alpha, z);
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fma(3.8284271247461900976, (double)i, 1.0);
+  uint32_t conv = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  for (int it = 0; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      if (!((conv >> j) & 1u)) {
+        double az = cabs(z[j]);
+        bool rev = az > 1.0;
+        cd x = rev ? crecip(z[j]) : z[j];
+        cd h, hd;
+        double b;
+        horner_pair<DEG>(p, alpha, x, rev ? 1.0 / az : az, rev, h, hd, b);
+        if (cabs(h) > CGB_EPS64 * b)
+          z[j] = z[j] - aberth_corr<DEG>(z, j, h, hd, rev);
+        else
+          conv |= 1u << j;
+      }
+    }
+    if (conv == all) return it + 1;
+  }
+  return -1;
+}
+
+// Compensated Horner (error-free transforms) for p and p' at x, optionally with
+// a low-order coefficient part pl (double-float coefficients).  Returns the
+// compensated h, hd and the running error bound eb (horner.h:281-385).
+template <int DEG, typename C, typename R>
+__device__ __forceinline__ void horner_comp(const C (&p)[DEG + 1], const C (&pl)[DEG + 1], bool use_lo, C x,
+                                            bool rev, C &h_out, C &hd_out, R &eb) {
+  C H = rev ? p[0] : p[DEG];
+  C e = use_lo ? (rev ? pl[0] : pl[DEG]) : H - H;
+  C D = H - H, ed = H - H;
+  R ax = sqrt(x.x * x.x + x.y * x.y);
+  eb = 0;
+#pragma unroll
+  for (int k = 1; k <= DEG; ++k) {
+    C pk = rev ? p[k] : p[DEG - k];
+    // D*x + H
+    R p0, q0, p1, q1, p2, q2, p3, q3, s4, r4, s5, r5, sx, ex, sy, ey;
+    two_prod(D.x, x.x, p0, q0);
+    two_prod(D.y, x.y, p1, q1);
+    two_prod(D.x, x.y, p2, q2);
+    two_prod(D.y, x.x, p3, q3);
+    two_sum(p0, -p1, s4, r4);
+    two_sum(p2, p3, s5, r5);
+    two_sum(s4, H.x, sx, ex);
+    two_sum(s5, H.y, sy, ey);
+    D = C{sx, sy};
+    ed = cfma(ed, x, e) + C{(q0 - q1) + (r4 + ex), (q2 + q3) + (r5 + ey)};
+    // H*x + p_k
+    two_prod(H.x, x.x, p0, q0);
+    two_prod(H.y, x.y, p1, q1);
+    two_prod(H.x, x.y, p2, q2);
+    two_prod(H.y, x.x, p3, q3);
+    two_sum(p0, -p1, s4, r4);
+    two_sum(p2, p3, s5, r5);
+    two_sum(s4, pk.x, sx, ex);
+    two_sum(s5, pk.y, sy, ey);
+    H = C{sx, sy};
+    C lo = C{(q0 - q1) + (r4 + ex), (q2 + q3) + (r5 + ey)};
+    if (use_lo) lo = lo + (rev ? pl[k] : pl[DEG - k]);
+    e = cfma(e, x, lo);
+    eb = eb * ax + (fabs(q0) + fabs(q1) + fabs(q2) + fabs(q3) + fabs(r4) + fabs(r5) + fabs(ex) + fabs(ey));
+  }
+  h_out = H + e;
+  hd_out = D + ed;
+}
+
+template <typename R>
+__device__ __forceinline__ R gamma_const(unsigned n, R eps) {
+  R g = (R)(2 * n) * eps * (R)1.41421356237309504880;
+  return g / (((R)1 - (R)2 * eps) - g);
+}
+
+// The reference's compensated solver: stage 1 as aberth64, stage 2 with the
+// compensated error bound (ehrlich_aberth.h:229-273).
+template <int DEG>
+__device__ int aberth64_comp(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
+  double alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = cabs(p[i]);
+  if (!warm) init_estimates<DEG>(alpha, z);
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fma(3.8284271247461900976, (double)i, 1.0);
+  uint32_t cx = 0, cy = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  const double gam = gamma_const<double>(4 * DEG + 2, CGB_EPS64);
+  for (int it = 0; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      double az = cabs(z[j]);
+      bool rev = az > 1.0;
+      cd x = rev ? crecip(z[j]) : z[j];
+      if (!((cx >> j) & 1u)) {
+        cd h, hd;
+        double b;
+        horner_pair<DEG>(p, alpha, x, rev ? 1.0 / az : az, rev, h, hd, b);
+        if (cabs(h) > CGB_EPS64 * b)
+          z[j] = z[j] - aberth_corr<DEG>(z, j, h, hd, rev);
+        else
+          cx |= 1u << j;
+      } else if (!((cy >> j) & 1u)) {
+        cd h, hd;
+        double eb;
+        horner_comp<DEG, cd, double>(p, p, false, x, rev, h, hd, eb);
+        double ah = cabs(h);
+        double bound = CGB_EPS64 * ah + (gam * eb + 2 * CGB_EPS64 * CGB_EPS64 * ah);
+        if (ah > 4 * bound) {
+          cd c = aberth_corr<DEG>(z, j, h, hd, rev);
+          double lim = rev ? 4 * CGB_EPS64 * az : 4 * CGB_EPS64;
+          if (cabs(c) > lim)
+            z[j] = z[j] - c;
+          else
+            cy |= 1u << j;
+        } else {
+          cy |= 1u << j;
+        }
+      }
+    }
+    if (cy == all) return it + 1;
+  }
+  return -1;
+}
+
+// Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
+// polynomial, FP64 Newton polish, FP64 fallback.  Returns the FP32 iteration
+// count, -1 on non-convergence; sets CGB_ST_FALLBACK in flags when used.
+template <int DEG>
+__device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
+  cf ph[DEG + 1], pl[DEG + 1];
+  float alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) {
+    ph[i] = tof(p[i]);
+    pl[i] = tof(p[i] - tod(ph[i]));
+    alpha[i] = cabs(ph[i]);
+  }
+  if (!warm) init_estimates<DEG>(alpha, z);
+  cf zf[DEG];
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
+  const float gam = gamma_const<float>(4 * DEG + 2, CGB_EPS32);
+  uint32_t cx = 0, cy = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  int it = 0;
+  for (; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      float az = cabs(zf[j]);
+      bool rev = az > 1.0f;
+      cf x = rev ? crecip(zf[j]) : zf[j];
+      if (!((cx >> j) & 1u)) {
+        cf h, hd;
+        float b;
+        horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+        if (cabs(h) > CGB_EPS32 * b)
+          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
+        else
+          cx |= 1u << j;
+      } else if (!((cy >> j) & 1u)) {
+        cf h, hd;
+        float eb;
+        horner_comp<DEG, cf, float>(ph, pl, true, x, rev, h, hd, eb);
+        float ah = cabs(h);
+        float bound = CGB_EPS32 * ah + (gam * eb + 2 * CGB_EPS32 * CGB_EPS32 * ah);
+        if (ah > 4 * bound) {
+          cf c = aberth_corr<DEG>(zf, j, h, hd, rev);
+          if (cabs(c) > 4 * CGB_EPS32 * az)
+            zf[j] = zf[j] - c;
+          else
+            cy |= 1u << j;
+        } else {
+          cy |= 1u << j;
+        }
+      }
+    }
+    if (cy == all) break;
+  }
+  bool ok = (cy == all) && isfinite(zf[0].x);
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) z[i] = tod(zf[i]);
+  // FP64 Newton polish (forward Horner; degrees are small)
+  double worst = 0.0;
+  for (int sweep = 0; sweep < 3 && ok; ++sweep) {
+    worst = 0.0;
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      cd h = p[DEG], hd = mk(0, 0);
+#pragma unroll
+      for (int k = DEG - 1; k >= 0; --k) {
+        hd = cfma(hd, z[j], h);
+        h = cfma(h, z[j], p[k]);
+      }
+      cd c = cdiv(h, hd);
+      z[j] = z[j] - c;
+      double rel = norm2(c) / fmax(norm2(z[j]), 1e-300);
+      worst = fmax(worst, rel);
+    }
+    if (!(worst <= 8.271806125530277e-25)) continue;  // |corr| <= 2^-40 |z|
+    break;
+  }
+  ok = ok && (worst <= 8.271806125530277e-25);
+  // distinct roots (Newton alone may merge a near-double pair)
+  if (ok) {
+    double scale = 0.0;
+#pragma unroll
+    for (int i = 0; i < DEG; ++i) scale = fmax(scale, norm2(z[i]));
+#pragma unroll
+    for (int i = 0; i < DEG; ++i)
+#pragma unroll
+      for (int k = i + 1; k < DEG; ++k)
+        if (norm2(z[i] - z[k]) < 1e-14 * scale) ok = false;
+  }
+  if (!ok) {
+    flags |= CGB_ST_FALLBACK;
+    int it64 = aberth64<DEG>(p, z, itmax, true);
+    if (it64 < 0) {
+      // restart cold in FP64 once before reporting failure
+      it64 = aberth64<DEG>(p, z, itmax, false);
+      if (it64 < 0) return -1;
+    }
+  }
+  return it + 1;
+}

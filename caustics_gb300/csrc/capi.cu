@@ -1,0 +1,233 @@
+// C ABI of libcaustics_gb300 (declared in include/caustics_gb300.h).
+//
+// Every entry point takes caller-owned device buffers and a cudaStream_t,
+// launches asynchronously, never synchronises the device, never allocates, and
+// returns an int status (0 = launched).  Errors never cross the ABI as C++
+// exceptions; the message of the last failure on the calling thread is
+// available from cgb_last_error().
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "../../include/caustics_gb300.h"
+#include "es.h"
+#include "internal.h"
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, const char *detail = "") {
+  snprintf(g_err, sizeof(g_err), fmt, detail);
+  return code;
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return CGB_OK;
+  snprintf(g_err, sizeof(g_err), "%s: %s", what, cudaGetErrorString(e));
+  return CGB_ERR_CUDA;
+}
+
+bool lens_ok(const cgb_lens_params &p) {
+  if (p.nlenses != 2 && p.nlenses != 3) return false;
+  if (!(p.s > 0) || !(p.q > 0) || !isfinite(p.s) || !isfinite(p.q)) return false;
+  if (p.nlenses == 3 && (!(p.q3 >= 0) || !isfinite(p.r3) || !isfinite(p.psi))) return false;
+  return true;
+}
+
+Lens lens_of(const cgb_lens_params &p) { return make_lens(p.nlenses, p.s, p.q, p.q3, p.r3, p.psi); }
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+namespace cgb {
+
+void gauss_legendre(int n, double *x, double *w) {
+  // Newton iteration on P_n from the Chebyshev-like first guess, with the
+  // three-term recurrence for P_n and P_n' (Golub-Welsch nodes, classic form)
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = cos(pi * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1.0, p0 = 0.0;
+      for (int k = 0; k < n; ++k) {
+        double p2 = p0;
+        p0 = p1;
+        p1 = ((2.0 * k + 1.0) * z * p0 - k * p2) / (k + 1.0);
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) {
+        // one more evaluation of the derivative at the converged node
+        p1 = 1.0;
+        p0 = 0.0;
+        for (int k = 0; k < n; ++k) {
+          double p2 = p0;
+          p0 = p1;
+          p1 = ((2.0 * k + 1.0) * z * p0 - k * p2) / (k + 1.0);
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        break;
+      }
+    }
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_options *o, EsParams &P) {
+  if (!o) return fail(CGB_ERR_INVALID, "options pointer is null%s");
+  if (!lens_ok(lens)) return fail(CGB_ERR_INVALID, "invalid lens parameters%s");
+  if (!(rho > 0) || !isfinite(rho)) return fail(CGB_ERR_INVALID, "rho must be positive and finite%s");
+  if (o->npts_limb < 8) return fail(CGB_ERR_INVALID, "npts_limb must be >= 8%s");
+  if (o->limb_darkening && (o->npts_ld < 2 || o->npts_ld > 2 * GL_MAX))
+    return fail(CGB_ERR_INVALID, "npts_ld must be in [2, 128]%s");
+  if (o->precision != CGB_PREC_FP64 && o->precision != CGB_PREC_MIXED)
+    return fail(CGB_ERR_INVALID, "extended source precision must be FP64 or MIXED%s");
+  memset(&P, 0, sizeof(P));
+  P.L = lens_of(lens);
+  P.rho = rho;
+  P.u1 = o->limb_darkening ? o->u1 : 0.0;
+  P.niter = 10;
+  P.n0 = (int)(0.5 * o->npts_limb);
+  P.n_add = (int)((int)(0.5 * o->npts_limb) / P.niter);
+  P.Lcap = P.n0 + P.niter * P.n_add;
+  const int deg = lens.nlenses * lens.nlenses + 1;
+  P.CPcap = deg * (P.Lcap + 1) + 8;
+  P.ld = o->limb_darkening ? 1 : 0;
+  P.itmax = o->roots_itmax > 0 ? o->roots_itmax : 2500;
+  if (P.ld) {
+    P.n1 = o->npts_ld / 2;
+    P.n2 = o->npts_ld - P.n1;
+    gauss_legendre(P.n1, P.gl_x[0], P.gl_w[0]);
+    gauss_legendre(P.n2, P.gl_x[1], P.gl_w[1]);
+  }
+  if (P.Lcap > 4096) return fail(CGB_ERR_UNSUPPORTED, "npts_limb too large (limb buffer > 4096 points)%s");
+  size_t smem = es_smem_bytes(P, lens.nlenses);
+  int dev = 0, maxsmem = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (maxsmem > 0 && smem + 4096 > (size_t)maxsmem)
+    return fail(CGB_ERR_UNSUPPORTED, "npts_limb too large for shared memory%s");
+  return CGB_OK;
+}
+
+}  // namespace cgb
+
+using namespace cgb;
+
+extern "C" {
+
+const char *cgb_last_error(void) { return g_err; }
+
+int32_t cgb_abi_version(void) { return CGB_ABI_VERSION; }
+
+int cgb_gauss_legendre(int32_t n, double *x, double *w) {
+  if (n < 1 || n > 4096 || !x || !w) return fail(CGB_ERR_INVALID, "invalid Gauss-Legendre request%s");
+  gauss_legendre(n, x, w);
+  return CGB_OK;
+}
+
+int cgb_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int32_t deg,
+                 int32_t itmax, int32_t precision, uint32_t *status, void *stream) {
+  if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
+  if (n > 0 && (!coeffs || !roots)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (deg != 4 && deg != 5 && deg != 6 && deg != 10)
+    return fail(CGB_ERR_UNSUPPORTED, "degree must be 4, 5, 6 or 10%s");
+  if (precision < 0 || precision > 2) return fail(CGB_ERR_INVALID, "unknown precision%s");
+  if (itmax < 1) return fail(CGB_ERR_INVALID, "itmax must be >= 1%s");
+  return cuda_status(launch_ea_solve(coeffs, roots_init, roots, n, deg, itmax, precision, status,
+                                     (cudaStream_t)stream),
+                     "cgb_ea_solve launch");
+}
+
+// The reference's XLA GPU custom call: buffers[0] coeffs complex128[size, deg+1]
+// (low -> high), buffers[1] roots complex128[size*deg]; opaque is the packed
+// {int size, deg, itmax; bool compensated} descriptor (lib/ehrlich_aberth/kernels.h:11-17).
+void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t opaque_len) {
+  struct Descriptor {
+    int size, deg, itmax;
+    bool compensated;
+  } d;
+  if (opaque_len != sizeof(Descriptor) || !buffers) {
+    fail(CGB_ERR_INVALID, "gpu_ehrlich_aberth: invalid opaque descriptor size%s");
+    return;
+  }
+  memcpy(&d, opaque, sizeof(d));
+  cgb_ea_solve((const double *)buffers[0], nullptr, (double *)buffers[1], d.size, d.deg, d.itmax,
+               d.compensated ? CGB_PREC_FP64_COMP : CGB_PREC_FP64, nullptr, stream);
+}
+
+int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t *image_mask, int64_t n,
+                         cgb_lens_params lens, int32_t itmax, int32_t precision, uint32_t *status, void *stream) {
+  if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
+  if (n > 0 && (!w || !mag)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!lens_ok(lens)) return fail(CGB_ERR_INVALID, "invalid lens parameters%s");
+  if (precision < 0 || precision > 2) return fail(CGB_ERR_INVALID, "unknown precision%s");
+  if (itmax < 1) return fail(CGB_ERR_INVALID, "itmax must be >= 1%s");
+  return cuda_status(launch_mag_ps(lens_of(lens), w, mag, images, image_mask, n, itmax, precision, status,
+                                   (cudaStream_t)stream),
+                     "cgb_mag_point_source launch");
+}
+
+int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                            const cgb_es_options *opts, uint32_t *status, void *stream) {
+  if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
+  if (n > 0 && (!w0 || !mag)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  EsParams P;
+  int rc = make_es_params(lens, rho, opts, P);
+  if (rc) return rc;
+  int grid = opts->grid > 0 ? opts->grid : (int)((n < 8 * sm_count()) ? n : 8 * sm_count());
+  if (grid < 1) grid = 1;
+  return cuda_status(launch_es(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),
+                     "cgb_mag_extended_source launch");
+}
+
+int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                              const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream) {
+  if (n < 0 || (n > 0 && (!w0 || !mag || !dbg))) return fail(CGB_ERR_INVALID, "invalid buffers%s");
+  EsParams P;
+  int rc = make_es_params(lens, rho, opts, P);
+  if (rc) return rc;
+  P.dbg = dbg;
+  int grid = opts->grid > 0 ? opts->grid : (int)((n < 8 * sm_count()) ? n : 8 * sm_count());
+  if (grid < 1) grid = 1;
+  return cuda_status(launch_es(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),
+                     "cgb_debug_extended_source launch");
+}
+
+int64_t cgb_debug_record_len(int32_t npts_limb) {
+  int n0 = (int)(0.5 * npts_limb);
+  return ES_DBG_STRIDE(n0 + 10 * (n0 / 10));
+}
+
+int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+            const cgb_es_options *opts, uint32_t *status, void *stream) {
+  if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
+  if (n > 0 && (!w || !mag || !route)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  EsParams P;
+  int rc = make_es_params(lens, rho, opts, P);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int prec_ps = opts->precision == CGB_PREC_MIXED ? MIXED : FP64;
+  rc = cuda_status(launch_lc_points(P.L, lens.q, w, rho, mag, route, n, P.itmax, prec_ps, status, s),
+                   "cgb_mag point pass launch");
+  if (rc) return rc;
+  int grid = opts->grid > 0 ? opts->grid : (int)((n < 8 * sm_count()) ? n : 8 * sm_count());
+  if (grid < 1) grid = 1;
+  return cuda_status(launch_es_routed(P, w, route, n, mag, status, opts->precision, grid, s),
+                     "cgb_mag contour pass launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,24 @@
+// Host-side launchers shared between the translation units of the library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lens.cuh"
+
+namespace cgb {
+
+enum Precision : int { FP64 = 0, MIXED = 1, FP64_COMP = 2 };
+
+cudaError_t launch_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int deg,
+                            int itmax, int precision, uint32_t *status, cudaStream_t stream);
+
+cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *images, uint32_t *image_mask,
+                          int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream);
+
+// Light-curve point pass: images, hexadecapole, proximity (+ planetary when
+// q < 0.01) tests.  Writes mu_multi (the hexadecapole magnification) into mag and
+// route[i] = 1 where the full contour integration is needed.
+cudaError_t launch_lc_points(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
+                             int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream);
+
+}  // namespace cgb

@@ -1,0 +1,205 @@
+// Point-source kernels: the Ehrlich-Aberth solver as a batched primitive
+// (replaces the XLA custom call of lib/ehrlich_aberth/kernels.cc.cu:14-42),
+// fused point-source magnification (src/caustics/point_source.py:1652-1830), and
+// the per-point pass of the light-curve driver (src/caustics/lightcurve.py:99-227).
+//
+// One polynomial per thread with roots and coefficients in registers.  Global
+// traffic is staged through shared memory so that every warp moves contiguous
+// 16-byte words (coefficients in, roots out).
+#include "aberth.cuh"
+#include "hexadecapole.cuh"
+#include "internal.h"
+
+namespace cgb {
+
+constexpr int PS_THREADS = 128;
+
+template <int DEG>
+__device__ __forceinline__ int solve(int precision, const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm,
+                                     uint32_t &flags) {
+  if (precision == MIXED) return aberth_mixed<DEG>(p, z, itmax, warm, flags);
+  if (precision == FP64_COMP) return aberth64_comp<DEG>(p, z, itmax, warm);
+  return aberth64<DEG>(p, z, itmax, warm);
+}
+
+// coeffs: complex128 [n, DEG+1] low->high; roots_init: complex128 [n, DEG] or null.
+template <int DEG>
+__global__ void __launch_bounds__(PS_THREADS) ea_solve_kernel(const cd *__restrict__ coeffs,
+                                                              const cd *__restrict__ roots_init,
+                                                              cd *__restrict__ roots, int64_t n, int itmax,
+                                                              int precision, uint32_t *__restrict__ status) {
+  __shared__ cd stage[PS_THREADS * (DEG + 1)];
+  const int64_t base = (int64_t)blockIdx.x * PS_THREADS;
+  const int tid = threadIdx.x;
+  const int64_t cnt = min((int64_t)PS_THREADS, n - base);
+  // coalesced load of this block's coefficients
+  for (int i = tid; i < cnt * (DEG + 1); i += PS_THREADS) stage[i] = coeffs[base * (DEG + 1) + i];
+  __syncthreads();
+  cd p[DEG + 1], z[DEG];
+  bool active = tid < cnt;
+  if (active) {
+#pragma unroll
+    for (int k = 0; k <= DEG; ++k) p[k] = stage[tid * (DEG + 1) + k];
+  }
+  __syncthreads();
+  if (roots_init) {
+    for (int i = tid; i < cnt * DEG; i += PS_THREADS) stage[i] = roots_init[base * DEG + i];
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < DEG; ++k) z[k] = stage[tid * DEG + k];
+    }
+    __syncthreads();
+  }
+  uint32_t flags = 0;
+  if (active) {
+    int it = solve<DEG>(precision, p, z, itmax, roots_init != nullptr, flags);
+    if (it < 0) flags |= CGB_ST_NOCONV;
+#pragma unroll
+    for (int k = 0; k < DEG; ++k) stage[tid * DEG + k] = z[k];
+    if (status) status[base + tid] = flags;
+  }
+  __syncthreads();
+  for (int i = tid; i < cnt * DEG; i += PS_THREADS) roots[base * DEG + i] = stage[i];
+}
+
+cudaError_t launch_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int deg,
+                            int itmax, int precision, uint32_t *status, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+  const cd *c = reinterpret_cast<const cd *>(coeffs);
+  const cd *ri = reinterpret_cast<const cd *>(roots_init);
+  cd *r = reinterpret_cast<cd *>(roots);
+  switch (deg) {
+    case 4: ea_solve_kernel<4><<<grid, PS_THREADS, 0, stream>>>(c, ri, r, n, itmax, precision, status); break;
+    case 5: ea_solve_kernel<5><<<grid, PS_THREADS, 0, stream>>>(c, ri, r, n, itmax, precision, status); break;
+    case 6: ea_solve_kernel<6><<<grid, PS_THREADS, 0, stream>>>(c, ri, r, n, itmax, precision, status); break;
+    case 10: ea_solve_kernel<10><<<grid, PS_THREADS, 0, stream>>>(c, ri, r, n, itmax, precision, status); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// Images of one (shifted) source position; returns the real-image bit mask and
+// raises CGB_ST_AMBIGUOUS when a residual sits within x30 of the 1e-6 threshold.
+template <int NL>
+__device__ __forceinline__ uint32_t images(const Lens &L, cd w, cd (&z)[NL * NL + 1], int itmax, int precision,
+                                           uint32_t &flags) {
+  constexpr int DEG = NL * NL + 1;
+  cd p[DEG + 1];
+  lens_poly<NL>(L, w, p);
+  int it = solve<DEG>(precision, p, z, itmax, false, flags);
+  if (it < 0) flags |= CGB_ST_NOCONV;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) {
+    double r = cabs(lens_eq<NL>(L, z[i]) - w);
+    if (r < 1e-6) mask |= 1u << i;
+    if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
+  }
+  return mask;
+}
+
+template <int NL>
+__global__ void __launch_bounds__(PS_THREADS) mag_ps_kernel(Lens L, const cd *__restrict__ w, double *__restrict__ mag,
+                                                            cd *__restrict__ images_out,
+                                                            uint32_t *__restrict__ mask_out, int64_t n, int itmax,
+                                                            int precision, uint32_t *__restrict__ status) {
+  constexpr int DEG = NL * NL + 1;
+  __shared__ cd stage[PS_THREADS * DEG];
+  const int64_t base = (int64_t)blockIdx.x * PS_THREADS;
+  const int tid = threadIdx.x;
+  const int64_t i = base + tid;
+  const int64_t cnt = min((int64_t)PS_THREADS, n - base);
+  cd z[DEG];
+  uint32_t flags = 0, m = 0;
+  if (i < n) {
+    cd wi = w[i];
+    wi.x += L.x_cm;
+    m = images<NL>(L, wi, z, itmax, precision, flags);
+    double mu = 0.0;
+#pragma unroll
+    for (int k = 0; k < DEG; ++k)
+      if ((m >> k) & 1u) mu += 1.0 / fabs(lens_det<NL>(L, z[k]));
+    mag[i] = mu;
+    if (status) status[i] = flags;
+    if (mask_out) mask_out[i] = m;
+  }
+  if (images_out) {
+    if (i < n) {
+#pragma unroll
+      for (int k = 0; k < DEG; ++k) stage[tid * DEG + k] = z[k];
+    }
+    __syncthreads();
+    for (int j = tid; j < cnt * DEG; j += PS_THREADS) images_out[base * DEG + j] = stage[j];
+  }
+}
+
+cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *images_out, uint32_t *mask_out,
+                          int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+  const cd *wc = reinterpret_cast<const cd *>(w);
+  cd *im = reinterpret_cast<cd *>(images_out);
+  if (L.n == 2)
+    mag_ps_kernel<2><<<grid, PS_THREADS, 0, stream>>>(L, wc, mag, im, mask_out, n, itmax, precision, status);
+  else if (L.n == 3)
+    mag_ps_kernel<3><<<grid, PS_THREADS, 0, stream>>>(L, wc, mag, im, mask_out, n, itmax, precision, status);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// Per-point pass of mag(): binary lenses get the hexadecapole magnification and
+// the routing test; triple lenses always route to the contour integral
+// (lightcurve.py:226-227).
+template <int NL>
+__global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q, const cd *__restrict__ w, double rho,
+                                                               double *__restrict__ mag, uint8_t *__restrict__ route,
+                                                               int64_t n, int itmax, int precision,
+                                                               uint32_t *__restrict__ status) {
+  constexpr int DEG = NL * NL + 1;
+  const int64_t i = (int64_t)blockIdx.x * PS_THREADS + threadIdx.x;
+  if (i >= n) return;
+  uint32_t flags = 0;
+  cd wi = w[i];
+  wi.x += L.x_cm;
+  cd z[DEG];
+  uint32_t m = images<NL>(L, wi, z, itmax, precision, flags);
+  double mu_multi = 0.0, dmu = 0.0;
+  bool hex_ok = false;
+  if (NL == 2) {
+#pragma unroll
+    for (int k = 0; k < DEG; ++k) {
+      if (!((m >> k) & 1u)) continue;
+      cd W[5];
+      hexa::wk<NL>(L, z[k], W);
+      double mu0, dq, dh;
+      hexa::terms(W, rho, 0.0, mu0, dq, dh);
+      mu_multi += fabs(mu0 + dq + dh);
+      dmu += fabs(dq) + fabs(dh);
+    }
+    const cd(&z5)[5] = reinterpret_cast<const cd(&)[5]>(z);
+    hex_ok = proximity_test_binary(L, wi, z5, m, rho, dmu);
+    if (q < 0.01) hex_ok = hex_ok && planetary_test(L, wi, rho);
+  }
+  mag[i] = mu_multi;
+  route[i] = hex_ok ? 0 : 1;
+  if (status) status[i] = flags;
+}
+
+cudaError_t launch_lc_points(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
+                             int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+  const cd *wc = reinterpret_cast<const cd *>(w);
+  if (L.n == 2)
+    lc_points_kernel<2><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, precision, status);
+  else if (L.n == 3)
+    lc_points_kernel<3><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, precision, status);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace cgb

@@ -1,0 +1,129 @@
+/*
+ * caustics_gb300 — C ABI of the GB300 (sm_103a) magnification library.
+ *
+ * Drop-in boundary for the magnification hot path of fbartolic/caustics.  All
+ * pointers are caller-owned DEVICE buffers (complex128 = two interleaved
+ * doubles), `stream` is a cudaStream_t (NULL = legacy default stream).  Calls
+ * launch asynchronously on that stream, never synchronise the device, never
+ * allocate and never throw.  The return value is a launch status (CGB_OK or an
+ * error code, message in cgb_last_error()); per-item outcomes (convergence,
+ * ambiguous image counts, ...) are written as CGB_ST_* bits into the optional
+ * `status` buffer (uint32 per item) when the kernels run.
+ */
+#ifndef CAUSTICS_GB300_H
+#define CAUSTICS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGB_ABI_VERSION 1
+
+/* launch status */
+#define CGB_OK 0
+#define CGB_ERR_INVALID 1     /* bad argument (null buffer, negative size, bad lens, ...) */
+#define CGB_ERR_CUDA 2        /* CUDA launch error */
+#define CGB_ERR_UNSUPPORTED 3 /* valid but unsupported request (degree, buffer size) */
+
+/* arithmetic of the root solver / quadrature */
+#define CGB_PREC_FP64 0      /* the reference's FP64 Aberth iteration, FP64 quadrature */
+#define CGB_PREC_MIXED 1     /* FP32 Aberth + compensated double-float stage + FP64 polish; FP32 LD nodes */
+#define CGB_PREC_FP64_COMP 2 /* the reference's compensated FP64 Aberth */
+
+/* per-item status bits */
+#define CGB_ST_NOCONV 1u     /* a root solve reached itmax */
+#define CGB_ST_AMBIGUOUS 2u  /* a lens-equation residual within x30 of the 1e-6 image threshold */
+#define CGB_ST_FALLBACK 4u   /* the mixed solver fell back to FP64 Aberth */
+#define CGB_ST_MERGE 8u      /* contour linking left open segments / overflowed */
+#define CGB_ST_CAPACITY 16u  /* limb or contour buffers too small */
+
+/* Lens parameters exactly as the reference's keyword arguments:
+ * binary (nlenses=2): s, q;  triple (nlenses=3): s, q, q3, r3, psi
+ * (src/caustics/point_source.py:1763-1817). */
+typedef struct cgb_lens_params {
+  int32_t nlenses;
+  double s, q;
+  double q3, r3, psi;
+} cgb_lens_params;
+
+/* Options of mag_extended_source / mag (src/caustics/extended_source.py:741-752,
+ * src/caustics/lightcurve.py:99-110). */
+typedef struct cgb_es_options {
+  int32_t npts_limb;      /* reference defaults: 150 (mag_extended_source), 200 (mag) */
+  int32_t limb_darkening; /* 0 = uniform source, 1 = linear limb darkening */
+  double u1;              /* linear limb-darkening coefficient */
+  int32_t npts_ld;        /* Gauss-Legendre nodes per P/Q integral (2..128), reference default 100 */
+  int32_t roots_itmax;    /* reference default 2500 */
+  int32_t precision;      /* CGB_PREC_FP64 or CGB_PREC_MIXED */
+  int32_t grid;           /* CTAs to launch, 0 = automatic */
+} cgb_es_options;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *cgb_last_error(void);
+
+/* CGB_ABI_VERSION of the loaded library. */
+int32_t cgb_abi_version(void);
+
+/* Gauss-Legendre nodes (ascending) and weights on [-1, 1]; host-only, needs no
+ * GPU.  Replaces numpy.polynomial.legendre.leggauss in
+ * src/caustics/integrate.py:18-21. */
+int cgb_gauss_legendre(int32_t n, double *x, double *w);
+
+/* Roots of n polynomials of degree deg (4, 5, 6 or 10).
+ * coeffs: complex128[n, deg+1], low -> high order; roots: complex128[n, deg];
+ * roots_init: complex128[n, deg] warm start or NULL (cold start).
+ * Replaces the XLA custom calls cpu_ehrlich_aberth / gpu_ehrlich_aberth
+ * (lib/ehrlich_aberth/cpu_ops.cc:15-81, kernels.cc.cu:44-112) bound by the
+ * ehrlich_aberth primitive (src/caustics/ehrlich_aberth_primitive.py:98-244). */
+int cgb_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int32_t deg,
+                 int32_t itmax, int32_t precision, uint32_t *status, void *stream);
+
+/* The reference's legacy XLA GPU custom-call signature with its opaque
+ * descriptor {int size, deg, itmax; bool compensated}
+ * (lib/ehrlich_aberth/kernels.h:11-20, gpu_ops.cc:14-25): buffers[0] = coeffs,
+ * buffers[1] = roots.  Errors are reported through cgb_last_error(). */
+void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Point-source magnification of n source positions w (complex128[n], in the
+ * reference's centre-of-mass frame); mag: float64[n].  Optional outputs:
+ * images complex128[n, nlenses^2+1] and image_mask uint32[n] (bit i = image i
+ * passes |lens_eq(z) - w| < 1e-6).
+ * Replaces mag_point_source (src/caustics/point_source.py:1762-1830). */
+int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t *image_mask, int64_t n,
+                         cgb_lens_params lens, int32_t itmax, int32_t precision, uint32_t *status, void *stream);
+
+/* Extended-source magnification by contour integration for n source centres
+ * w0 (complex128[n]) of radius rho; mag: float64[n].
+ * Replaces mag_extended_source (src/caustics/extended_source.py:741-904). */
+int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                            const cgb_es_options *opts, uint32_t *status, void *stream);
+
+/* Light curve: hexadecapole where the reference's proximity tests accept it,
+ * contour integration elsewhere.  route: uint8[n] output, 1 where the contour
+ * integral was used.  Replaces mag (src/caustics/lightcurve.py:99-254). */
+int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+            const cgb_es_options *opts, uint32_t *status, void *stream);
+
+/* Diagnostics (no counterpart in the reference): cgb_mag_extended_source that
+ * also writes, per point, a record of cgb_debug_record_len(npts_limb) doubles:
+ * [L, n_contours, merge flags, (start, count, parity, integral) x 13,
+ *  theta of the L limb points in limb order]. */
+int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                              const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
+int64_t cgb_debug_record_len(int32_t npts_limb);
+
+/* Measurement utility (no counterpart in the reference): launches `blocks`
+ * CTAs of 256 threads, each thread running iters*16*8 dependent-free fused
+ * multiply-adds in FP32 (fp64 = 0) or FP64; flops = blocks*256*iters*256.
+ * `out` needs one element per block (never written in practice).  Used as the
+ * live FMA-pipe roofline denominator of the SIMT kernels. */
+int cgb_probe_fma(int32_t fp64, int32_t iters, int32_t blocks, void *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CAUSTICS_GB300_H */

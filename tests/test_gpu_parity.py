@@ -1,0 +1,200 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's
+golden fixtures and the oracle, on the same inputs.
+
+Tolerances: roots 1e-10 relative (root sets); point-source magnification
+1e-9 relative (binary; 1e-4 for ill-conditioned degree-10 triples);
+extended-source / light-curve magnification 1e-4 relative — the reference's own
+result moves by ~3e-5 under a different warm-start jitter seed.  Image counts
+must be equal except where a lens-equation residual is within x30 of the 1e-6
+threshold (flagged CGB_ST_AMBIGUOUS).
+"""
+import ctypes
+import struct
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import caustics_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+C = pytest.importorskip("caustics_gb300")
+from caustics_gb300 import _lib as L  # noqa: E402
+
+
+def setdist(a, b):
+    """max over roots of the distance to the nearest root of the other set, relative to max(|root|, 1)."""
+    d1 = np.min(np.abs(a[..., :, None] - b[..., None, :]), axis=-1)
+    d2 = np.min(np.abs(b[..., :, None] - a[..., None, :]), axis=-1)
+    scale = np.maximum(np.abs(b), 1.0)
+    return max(np.max(d1 / scale), np.max(d2 / scale))
+
+
+def ambiguous(z, w, lens):
+    res = np.abs(O.lens_eq(z, lens) - w[None, :])
+    return np.any((res > 1e-6 / 30) & (res < 1e-6 * 30), axis=0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_comp", "mixed"])
+def test_ea_solve_cfg1_roots(G, precision):
+    d = G("roots_cfg1")
+    c = np.ascontiguousarray(d["coeffs"][:, ::-1])
+    r = C.ehrlich_aberth(c, None, itmax=2500, precision=precision).reshape(c.shape[0], 5)
+    assert setdist(r, d["roots_plain"]) < 1e-10
+
+
+@pytest.mark.parametrize("comp", [False, True])
+def test_poly_roots_reference_fixture(G, comp):
+    """tests/test_ehrlich_aberth_primitive.py:30-35 on the reference's fixture."""
+    d = G("roots_fixture")
+    coeffs = d["coeffs"].reshape(5, 2, 6)
+    roots = C.poly_roots(coeffs, compensated=comp)
+    assert roots.shape == (5, 2, 5)
+    ev = np.polyval(coeffs[3, 1], roots[3, 1])
+    np.testing.assert_allclose(ev, np.zeros_like(ev), atol=1e-10)
+    assert setdist(roots.reshape(10, 5), O.ea_solve(d["coeffs"][:, ::-1], init_mode=0)) < 1e-10
+
+
+def test_poly_roots_warm_start(G):
+    d = G("roots_cfg1")
+    c = d["coeffs"][:64]
+    init = d["roots_plain"][:64] + 1e-3
+    r = C.poly_roots(c, custom_init=True, roots_init=init)
+    assert setdist(r, d["roots_plain"][:64]) < 1e-10
+
+
+def test_degree_4_6_10_random():
+    rng = np.random.default_rng(3)
+    for deg in (4, 6, 10):
+        c = rng.normal(size=(200, deg + 1)) + 1j * rng.normal(size=(200, deg + 1))
+        r = C.poly_roots(c)
+        ref = O.poly_roots(c, init_mode=0)
+        assert setdist(r, ref) < 1e-9
+
+
+def test_legacy_xla_custom_call(G):
+    """The reference's GPU custom-call ABI: buffers + packed descriptor."""
+    d = G("roots_cfg1")
+    c = torch.as_tensor(np.ascontiguousarray(d["coeffs"][:100, ::-1])).cuda()
+    out = torch.empty((100 * 5,), dtype=torch.complex128, device="cuda")
+    bufs = (ctypes.c_void_p * 2)(c.data_ptr(), out.data_ptr())
+    for comp in (False, True):
+        desc = struct.pack("iii?3x", 100, 5, 2500, comp)
+        L.lib().gpu_ehrlich_aberth(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), bufs, desc, len(desc))
+        torch.cuda.synchronize()
+        assert setdist(out.cpu().numpy().reshape(100, 5), d["roots_plain"][:100]) < 1e-10
+
+
+def test_invalid_arguments_rejected():
+    lib = L.lib()
+    rc = lib.cgb_ea_solve(None, None, None, 0, 7, 100, 0, None, None)
+    assert rc == L.CGB_ERR_UNSUPPORTED
+    rc = lib.cgb_ea_solve(None, None, None, 10, 5, 100, 0, None, None)
+    assert rc == L.CGB_ERR_INVALID
+    assert b"null" in lib.cgb_last_error()
+    bad = L.LensParams(4, 1.0, 0.1, 0, 0, 0)
+    assert lib.cgb_mag_point_source(None, None, None, None, 0, bad, 100, 0, None, None) == L.CGB_ERR_INVALID
+    opts = L.EsOptions(4, 0, 0.0, 100, 100, 0, 0)
+    good = L.LensParams(2, 1.0, 0.1, 0, 0, 0)
+    assert lib.cgb_mag_extended_source(None, None, 0, 0.01, good, opts, None, None) == L.CGB_ERR_INVALID
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mag_point_source_binary(G, precision):
+    for name, s, q in (("mag_ps_cfg1", 0.9, 0.1), ("mag_ps_grid", 0.9, 0.2)):
+        d = G(name)
+        m, z, mask, st = C.mag_point_source(d["w"], s=s, q=q, precision=precision, return_images=True,
+                                            return_status=True)
+        assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
+        assert not np.any(st & L.ST_NOCONV)
+        lens = O.Lens.binary(s, q)
+        zo, mo = O.images_point_source(d["w"] + lens.x_cm, lens)
+        cnt = np.array([bin(int(x)).count("1") for x in mask])
+        amb = ambiguous(zo, d["w"] + lens.x_cm, lens)
+        assert np.array_equal(cnt[~amb], mo.sum(0)[~amb])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mag_point_source_triple(G, precision):
+    d = G("mag_ps_triple")
+    for k in range(len(d["s1"])):
+        p = dict(s=d["s1"][k], q=d["q1"][k], q3=d["q2"][k], r3=d["s2"][k], psi=d["psi"][k])
+        m, z, mask = C.mag_point_source(d["w"][k], nlenses=3, precision=precision, return_images=True, **p)
+        assert np.max(np.abs(m - d["mag"][k]) / d["mag"][k]) < 1e-4
+        lens = O.Lens.triple(p["s"], p["q"], p["q3"], p["r3"], p["psi"])
+        w = d["w"][k] + lens.x_cm
+        amb = ambiguous(d["z"][k], w, lens) | ambiguous(np.moveaxis(z, -1, 0), w, lens)
+        cnt = np.array([bin(int(x)).count("1") for x in mask])
+        assert np.array_equal(cnt[~amb], d["mask"][k].sum(0)[~amb])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("k", range(6))
+def test_mag_extended_source_golden(G, k, precision):
+    d = G(f"mag_es{k}")
+    m, st = C.mag_extended_source(d["w"], float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=bool(d["ld"]),
+                                  u1=float(d["u1"]), s=float(d["s"]), q=float(d["q"]), precision=precision,
+                                  return_status=True)
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+    assert not np.any(st & (L.ST_NOCONV | L.ST_CAPACITY))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mag_extended_source_triple_golden(G, precision):
+    d = G("mag_es_triple")
+    m = C.mag_extended_source(d["w"], float(d["rho"]), nlenses=3, npts_limb=int(d["npts_limb"]), s=float(d["s"]),
+                              q=float(d["q"]), q3=float(d["q3"]), r3=float(d["r3"]), psi=float(d["psi"]),
+                              precision=precision)
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["mag_lc_cfg2", "mag_lc_q0.3"])
+def test_mag_light_curve_golden(G, name, precision):
+    d = G(name)
+    m, route = C.mag(d["w"], float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=True, u1=float(d["u1"]),
+                     npts_ld=int(d["npts_ld"]), s=float(d["s"]), q=float(d["q"]), precision=precision,
+                     return_route=True)
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+
+
+@pytest.mark.parametrize("tag", ["q0.2", "q5e-3", "q0.05"])
+def test_hexadecapole_routing(G, tag):
+    """Per-point hexadecapole magnification and routing against the reference's
+    _mag_hexadecapole / _caustics_proximity_test / _planetary_caustic_test."""
+    d = G("hex_" + tag)
+    q = float(d["q"])
+    test = d["test_prox"] & d["test_planet"] if q < 0.01 else d["test_prox"]
+    m, route = C.mag(d["w"], float(d["rho"]), npts_limb=60, limb_darkening=False, s=float(d["s"]), q=q,
+                     return_route=True)
+    assert np.array_equal(route, ~test)
+    ok = test
+    assert np.max(np.abs(m[ok] - d["mu_multi"][ok]) / d["mu_multi"][ok]) < 1e-10
+
+
+@pytest.mark.parametrize("ld", [False, True])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mag_extended_source_random_vs_oracle(ld, precision):
+    """Random lenses, points near caustics, several npts_limb, against the oracle."""
+    rng = np.random.default_rng(7 + ld)
+    for trial in range(4):
+        s = float(10 ** rng.uniform(np.log10(0.5), np.log10(2.0)))
+        q = float(10 ** rng.uniform(-3, 0))
+        rho = float(10 ** rng.uniform(-3, -1.3))
+        npts = int(rng.choice([60, 100, 200]))
+        _, cau = O.critical_and_caustic_curves(npts=40, s=s, q=q, init_mode=0)
+        c = cau.reshape(-1)
+        w = c[rng.choice(len(c), 4)] + rho * rng.uniform(0, 2, 4) * np.exp(1j * rng.uniform(0, 2 * np.pi, 4))
+        u1 = 0.6
+        ref = np.array([O.mag_extended_source(x, rho, npts_limb=npts, limb_darkening=ld, u1=u1, npts_ld=40, s=s, q=q)
+                        for x in w])
+        got = C.mag_extended_source(w, rho, npts_limb=npts, limb_darkening=ld, u1=u1, npts_ld=40, s=s, q=q,
+                                    precision=precision)
+        assert np.max(np.abs(got - ref) / ref) < 1e-4, (s, q, rho, npts, got, ref)
+
+
+def test_empty_inputs():
+    assert C.mag_point_source(np.zeros(0, dtype=complex), s=1.0, q=0.1).shape == (0,)
+    assert C.mag_extended_source(np.zeros(0, dtype=complex), 0.01, s=1.0, q=0.1).shape == (0,)
+    assert C.mag(np.zeros(0, dtype=complex), 0.01, s=1.0, q=0.1).shape == (0,)
