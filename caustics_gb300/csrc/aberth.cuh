@@ -29,8 +29,10 @@
 #define CGB_ST_MERGE 8u      // contour linking left open segments or overflowed its buffer
 #define CGB_ST_CAPACITY 16u  // limb / contour buffers too small for the request
 
+// real_guess: the reference's r*sin(phi) real initial guesses (init_est.h:95),
+// used only to reproduce the reference's labelling of roots.
 template <int DEG, typename R>
-__device__ __forceinline__ void init_estimates(const R (&alpha)[DEG + 1], cd (&z)[DEG]) {
+__device__ __forceinline__ void init_estimates(const R (&alpha)[DEG + 1], cd (&z)[DEG], bool real_guess = false) {
   double hx[DEG + 1], hy[DEG + 1], al[DEG + 1];
 #pragma unroll
   for (int i = 0; i <= DEG; ++i) al[i] = (double)alpha[i];
@@ -48,13 +50,14 @@ __device__ __forceinline__ void init_estimates(const R (&alpha)[DEG + 1], cd (&z
   int n = 0;
   for (int i = k - 2; i >= 0; --i) {
     int nz = (int)(hx[i] - hx[i + 1]);
-    double r = exp((hy[i + 1] - hy[i]) / nz);
+    double r = real_guess ? pow(al[(int)hx[i + 1]], 1.0 / nz) / pow(al[(int)hx[i]], 1.0 / nz)
+                          : exp((hy[i + 1] - hy[i]) / nz);
     if (!(r > 0.0) || !isfinite(r)) r = 1.0;
     double ang = pi2 / nz;
     for (int j = 0; j < nz && n + j < DEG; ++j) {
       double s, c;
       sincos(ang * j + th * i + 0.7, &s, &c);
-      t[n + j] = mk(r * c, r * s);
+      t[n + j] = real_guess ? mk(r * s, 0.0) : mk(r * c, r * s);
     }
     n += nz;
   }
@@ -91,11 +94,19 @@ __device__ __forceinline__ void horner_pair(const C (&p)[DEG + 1], const R (&alp
 }
 
 // Aberth correction; rev form from ehrlich_aberth.h:43-58
-template <int DEG, typename C>
+__device__ __forceinline__ cd sq_powform(cd z) {
+  // z^2 as thrust::pow(z, 2) = exp(2 log z) forms it (ehrlich_aberth.h:56-57)
+  double m = exp(2.0 * log(sqrt(z.x * z.x + z.y * z.y))), t = 2.0 * atan2(z.y, z.x), s, c;
+  sincos(t, &s, &c);
+  return mk(m * c, m * s);
+}
+__device__ __forceinline__ cf sq_powform(cf z) { return z * z; }
+
+template <int DEG, typename C, bool POWSQ = false>
 __device__ __forceinline__ C aberth_corr(const C (&z)[DEG], int j, C h, C hd, bool rev) {
   C s = aberth_sum<DEG, C>(z, j);
   if (rev) {
-    C z2h = z[j] * z[j] * h;
+    C z2h = (POWSQ ? sq_powform(z[j]) : z[j] * z[j]) * h;
     C d = z[j] * h;
     d = C{d.x * DEG, d.y * DEG} - hd - z2h * s;
     return cdiv(z2h, d);
@@ -103,12 +114,14 @@ __device__ __forceinline__ C aberth_corr(const C (&z)[DEG], int j, C h, C hd, bo
   return cdiv(h, hd - h * s);
 }
 
-template <int DEG>
+// REF: the reference's real initial guesses and pow-form square, to reproduce
+// its labelling of roots (row order) on a cold start.
+template <int DEG, bool REF = false>
 __device__ int aberth64(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
   double alpha[DEG + 1];
 #pragma unroll
   for (int i = 0; i <= DEG; ++i) alpha[i] = cabs(p[i]);
-  if (!warm) init_estimates<DEG>(alpha, z);
+  if (!warm) init_estimates<DEG>(alpha, z, REF);
 #pragma unroll
   for (int i = 0; i <= DEG; ++i) alpha[i] *= fma(3.8284271247461900976, (double)i, 1.0);
   uint32_t conv = 0;
@@ -124,7 +137,49 @@ __device__ int aberth64(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool wa
         double b;
         horner_pair<DEG>(p, alpha, x, rev ? 1.0 / az : az, rev, h, hd, b);
         if (cabs(h) > CGB_EPS64 * b)
-          z[j] = z[j] - aberth_corr<DEG>(z, j, h, hd, rev);
+          z[j] = z[j] - aberth_corr<DEG, cd, REF>(z, j, h, hd, rev);
+        else
+          conv |= 1u << j;
+      }
+    }
+    if (conv == all) return it + 1;
+  }
+  return -1;
+}
+
+// Plain FP32 Aberth (the reference's iteration with FP32 epsilon); used where
+// only the labelling of roots is needed (which iterate converges to which root).
+template <int DEG>
+__device__ int aberth32(const cd (&p64)[DEG + 1], cf (&zf)[DEG], int itmax, bool warm, bool real_guess) {
+  cf p[DEG + 1];
+  float alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) {
+    p[i] = tof(p64[i]);
+    alpha[i] = cabs(p[i]);
+  }
+  if (!warm) {
+    cd z[DEG];
+    init_estimates<DEG>(alpha, z, real_guess);
+#pragma unroll
+    for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
+  }
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
+  uint32_t conv = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  for (int it = 0; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      if (!((conv >> j) & 1u)) {
+        float az = cabs(zf[j]);
+        bool rev = az > 1.0f;
+        cf x = rev ? crecip(zf[j]) : zf[j];
+        cf h, hd;
+        float b;
+        horner_pair<DEG>(p, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+        if (cabs(h) > CGB_EPS32 * b)
+          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
         else
           conv |= 1u << j;
       }

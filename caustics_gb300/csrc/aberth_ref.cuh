@@ -1,0 +1,120 @@
+// FP64 Ehrlich-Aberth iteration with the reference's operation order and
+// rounding (lib/ehrlich_aberth/ehrlich_aberth.h:60-150, horner.h:219-267,
+// init_est.h:57-102): products and sums rounded one by one (no FMA
+// contraction), Smith's complex division, hypot for |z|, z^2 = exp(2 log z) in
+// the reversed correction, and the reference's real-valued initial guesses.
+//
+// It is used only where the reference's *labelling* of roots matters and is
+// decided by the iteration's dynamics: the first limb point's cold start and the
+// few warm-started limb steps whose nearest-root map is ambiguous.  The roots
+// themselves always come from the fast solvers in aberth.cuh.
+#pragma once
+#include "cplx.cuh"
+
+namespace refea {
+
+__device__ __forceinline__ cd mul(cd a, cd b) {
+  return cd{__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ cd add(cd a, cd b) { return cd{__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)}; }
+__device__ __forceinline__ cd sub(cd a, cd b) { return cd{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y)}; }
+__device__ __forceinline__ cd scale(cd a, double s) { return cd{__dmul_rn(a.x, s), __dmul_rn(a.y, s)}; }
+__device__ __forceinline__ double absc(cd a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ cd div(cd a, cd b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = __ddiv_rn(b.y, b.x), d = __dadd_rn(b.x, __dmul_rn(b.y, r));
+    return cd{__ddiv_rn(__dadd_rn(a.x, __dmul_rn(a.y, r)), d), __ddiv_rn(__dsub_rn(a.y, __dmul_rn(a.x, r)), d)};
+  }
+  double r = __ddiv_rn(b.x, b.y), d = __dadd_rn(__dmul_rn(b.x, r), b.y);
+  return cd{__ddiv_rn(__dadd_rn(__dmul_rn(a.x, r), a.y), d), __ddiv_rn(__dsub_rn(__dmul_rn(a.y, r), a.x), d)};
+}
+__device__ __forceinline__ cd recip(cd b) { return div(cd{1.0, 0.0}, b); }
+__device__ __forceinline__ cd sq_pow(cd z) {
+  double m = exp(__dmul_rn(2.0, log(absc(z)))), t = __dmul_rn(2.0, atan2(z.y, z.x));
+  return cd{__dmul_rn(m, cos(t)), __dmul_rn(m, sin(t))};
+}
+
+template <int DEG>
+__device__ void init_real(const double (&alpha)[DEG + 1], cd (&z)[DEG]) {
+  int hx[DEG + 1];
+  double hy[DEG + 1];
+  int k = 0;
+  for (int i = DEG; i >= 0; --i) {
+    double y = alpha[i] > 0 ? log(alpha[i]) : -1e30;
+    while (k >= 2) {
+      double ccw = __dsub_rn(__dmul_rn((double)(hx[k - 1] - hx[k - 2]), __dsub_rn(y, hy[k - 2])),
+                             __dmul_rn(__dsub_rn(hy[k - 1], hy[k - 2]), (double)(i - hx[k - 2])));
+      if (ccw <= 0) --k; else break;
+    }
+    hx[k] = i;
+    hy[k] = y;
+    ++k;
+  }
+  cd t[DEG];
+  const double pi2 = 6.28318530717958647693, th = __ddiv_rn(pi2, (double)DEG);
+  int n = 0;
+  for (int i = k - 2; i >= 0; --i) {
+    int nz = hx[i] - hx[i + 1];
+    double r = __ddiv_rn(pow(alpha[hx[i + 1]], __ddiv_rn(1.0, (double)nz)), pow(alpha[hx[i]], __ddiv_rn(1.0, (double)nz)));
+    double ang = __ddiv_rn(pi2, (double)nz);
+    for (int j = 0; j < nz && n + j < DEG; ++j) {
+      double phi = __dadd_rn(__dadd_rn(__dmul_rn(ang, (double)j), __dmul_rn(th, (double)i)), 0.7);
+      t[n + j] = cd{__dmul_rn(r, sin(phi)), 0.0};
+    }
+    n += nz;
+  }
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) z[i] = t[i];
+}
+
+// Returns the iteration count, -1 if itmax was reached.
+template <int DEG>
+__device__ int solve(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
+  double alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = absc(p[i]);
+  if (!warm) init_real<DEG>(alpha, z);
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = __dmul_rn(alpha[i], fma(3.8284271247461900976, (double)i, 1.0));
+  uint32_t conv = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  const double EPS = 1.1102230246251565e-16;
+  for (int it = 0; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      if ((conv >> j) & 1u) continue;
+      double az = absc(z[j]);
+      bool rev = az > 1.0;
+      cd x = rev ? recip(z[j]) : z[j];
+      double ax = rev ? __ddiv_rn(1.0, az) : az;
+      double b = rev ? alpha[0] : alpha[DEG];
+      cd h = rev ? p[0] : p[DEG], hd = cd{0.0, 0.0};
+#pragma unroll
+      for (int k = 1; k <= DEG; ++k) {
+        b = fma(b, ax, rev ? alpha[k] : alpha[DEG - k]);
+        hd = add(mul(hd, x), h);
+        h = add(mul(h, x), rev ? p[k] : p[DEG - k]);
+      }
+      if (absc(h) > __dmul_rn(EPS, b)) {
+        cd s = cd{0.0, 0.0};
+#pragma unroll
+        for (int i = 0; i < DEG; ++i)
+          if (i != j) s = add(s, recip(sub(z[j], z[i])));
+        cd corr;
+        if (rev) {
+          cd z2h = mul(sq_pow(z[j]), h);
+          corr = div(z2h, sub(sub(scale(mul(z[j], h), (double)DEG), hd), mul(z2h, s)));
+        } else {
+          corr = div(h, sub(hd, mul(h, s)));
+        }
+        z[j] = sub(z[j], corr);
+      } else {
+        conv |= 1u << j;
+      }
+    }
+    if (conv == all) return it + 1;
+  }
+  return -1;
+}
+
+}  // namespace refea

@@ -9,6 +9,18 @@ namespace cgb {
 
 constexpr int GL_MAX = 64;  // Gauss-Legendre nodes per half interval
 
+// Per-curve parameters of batched light curves (mirrors cgb_curve_params).
+struct CurveDev {
+  double s, q, rho, u1, u0, alpha, t0, tE;
+};
+
+// The lens / source of the item a CTA is integrating.
+struct EsItem {
+  Lens L;
+  double rho, u1;
+  cd w0;  // source centre, shifted by x_cm
+};
+
 struct EsParams {
   Lens L;
   double rho, u1;
@@ -20,12 +32,26 @@ struct EsParams {
   int ld;      // limb darkening on
   int n1, n2;  // Gauss-Legendre nodes on [a, split] and [split, b] (npts_ld/2 and the rest)
   int itmax;
+  // batched light curves (null for a single lens): point i belongs to the curve
+  // c with offsets[c] <= i < offsets[c+1]; its source is on the rectilinear
+  // trajectory at times[i] (trajectory.py:152-155 with pi_E = 0)
+  const CurveDev *curves;
+  const int64_t *offsets;
+  const double *times;
+  int64_t ncurves;
+  // persistent work queue (null: static round-robin over items)
+  unsigned long long *qhead;  // next item to take
+  const int64_t *qcount;      // number of queued items
+  const int64_t *qlist;       // queued point indices
+  int qchunk;                 // items taken per grab
   double *dbg;  // optional per-point diagnostics (cgb_debug_extended_source), stride ES_DBG_STRIDE(Lcap)
   double gl_x[2][GL_MAX], gl_w[2][GL_MAX];
 };
 
-// diagnostics record: [L, ncont, flags, (start, count, parity, integral) x 13, theta[0..L)]
-#define ES_DBG_HEAD (3 + 4 * 13)
+// diagnostics record: [L, ncont, flags, (start, count, parity, integral) x 13,
+// clock64 at the end of phases A..F (6) and the start (1) + 1 spare, theta[0..L)]
+#define ES_DBG_CLK (3 + 4 * 13)
+#define ES_DBG_HEAD (ES_DBG_CLK + 8)
 #define ES_DBG_STRIDE(lcap) (ES_DBG_HEAD + (lcap))
 
 size_t es_smem_bytes(const EsParams &P, int nl);

@@ -1,957 +1,37 @@
-// Extended-source magnification by contour integration, one CTA per source
-// position (src/caustics/extended_source.py:56-904, integrate.py:18-121).
-//
-// Phases inside a CTA (256 threads), all state in shared memory:
-//  A  n0 = npts/2 limb points solved in parallel (cold start), rows ordered by
-//     chained greedy matching (extended_source.py:34-53, utils.py:15-40);
-//  B  10 refinement rounds: gap per interval = max over images |dz| where either
-//     end is a real image, the n_add largest gaps (ties: larger index first, as
-//     argsort(...)[::-1]) get a midpoint solve warm-started from the left
-//     neighbour (extended_source.py:109-135);
-//  C  final chained matching over all limb points: every step's nearest-image
-//     map is computed in parallel; steps whose map is injective compose as
-//     permutations, the rest redo the greedy pass in track order;
-//  D  tracks -> closed tracks / split open segments (extended_source.py:156-309);
-//  E  segment linking into <= 3 contours (extended_source.py:312-727);
-//  F  Green's-theorem integral: trapezoid (uniform) or the Dominik (1998) P/Q
-//     line integrals with split Gauss-Legendre quadrature (integrate.py:47-121),
-//     one warp per contour point, FP64 or FP32 (shifted lens equation) nodes.
-#include "aberth.cuh"
+// Extended-source dispatch (src/caustics/extended_source.py:741-904): picks the
+// kernel variant for the lens multiplicity and the precision.  The kernel
+// itself is in es_kernel.cuh; each variant is compiled in its own translation
+// unit (es_b64.cu, es_b32.cu, es_t64.cu, es_t32.cu).
 #include "es.h"
 #include "internal.h"
+#include "es_kernel.cuh"
 
 namespace cgb {
 
-constexpr int ES_THREADS = 256;
-constexpr int ES_WARPS = ES_THREADS / 32;
-constexpr int MAX_SEG = 30;      // 3 * n_images for triple lenses
-constexpr int MAX_PIECES = 24;   // 1 + up to 20 merges per contour
-constexpr int N_CONTOURS = 3;    // merged contours (extended_source.py:871)
-constexpr int MAX_CLOSED = 10;
-
-struct Piece {
-  int16_t t, l, r;  // track, [l, r) positions
-  int16_t dir;      // +1 forward, -1 reversed
-};
-
-struct Segment {
-  int16_t t, l, r;
-  int16_t par;  // parity of the head point (+1 / -1), 0 for an empty segment
-  double len;   // path length
-  int alive;
-};
-
-struct MergeState {
-  Segment seg[MAX_SEG];
-  int order[MAX_SEG];
-  int nseg;
-  Piece pieces[N_CONTOURS][MAX_PIECES];
-  int npieces[N_CONTOURS];
-  int cpar[N_CONTOURS];
-  int cnpts[N_CONTOURS];
-  int closed_tracks[MAX_CLOSED];
-  int nclosed;
-  int all_closed;
-  uint32_t flags;
-};
-
-// shared-memory layout for one CTA
-template <int DEG>
-struct EsSmem {
-  cd *Z;          // [Lcap][DEG] roots per slot (rows)
-  double *TH;     // [Lcap] theta per slot
-  uint16_t *MK;   // [Lcap] real-image bits per slot (by row)
-  uint16_t *PP;   // [Lcap] positive-parity bits per slot (by row)
-  uint16_t *ZP;   // [Lcap] zero-det bits (parity 0)
-  uint16_t *ORD;  // [Lcap] position -> slot
-  uint16_t *ORD2;
-  uint64_t *PERM; // [Lcap] packed 4-bit permutation: track -> row
-  double *KEY;    // [Lcap]
-  int *SCAN;      // [Lcap + 1]
-  uint32_t *CP;   // [CPcap] contour points: slot * DEG + row
-  MergeState *M;
-};
-
-__device__ __forceinline__ int perm_get(uint64_t p, int t) { return (int)((p >> (4 * t)) & 15u); }
-__device__ __forceinline__ uint64_t perm_set(uint64_t p, int t, int v) {
-  return (p & ~(15ull << (4 * t))) | ((uint64_t)v << (4 * t));
-}
-
-// greedy nearest matching of rows b against a (processing order = a's order):
-// returns packed res[i] = b row matched to a[i]
-template <int DEG>
-__device__ uint64_t greedy_match(const cd *a, const cd *b) {
-  uint32_t taken = 0;
-  uint64_t res = 0;
-  for (int i = 0; i < DEG; ++i) {
-    int best = 0;
-    double bd = INFINITY;
-    bool found = false;
-    for (int j = 0; j < DEG; ++j) {
-      if ((taken >> j) & 1u) continue;
-      double d = norm2(b[j] - a[i]);
-      if (!found || d < bd) {
-        bd = d;
-        best = j;
-        found = true;
-      }
-    }
-    taken |= 1u << best;
-    res = perm_set(res, i, best);
-  }
-  return res;
-}
-
-// nearest row of b for every row of a; ok = the map is injective (then the
-// greedy result does not depend on the processing order)
-template <int DEG>
-__device__ uint64_t nearest_map(const cd *a, const cd *b, bool &ok) {
-  uint64_t res = 0;
-  uint32_t used = 0;
-  ok = true;
-  for (int i = 0; i < DEG; ++i) {
-    int best = 0;
-    double bd = norm2(b[0] - a[i]);
-    for (int j = 1; j < DEG; ++j) {
-      double d = norm2(b[j] - a[i]);
-      if (d < bd) {
-        bd = d;
-        best = j;
-      }
-    }
-    if ((used >> best) & 1u) ok = false;
-    used |= 1u << best;
-    res = perm_set(res, i, best);
-  }
-  return res;
-}
-
-// block-wide exclusive scan of SCAN[0..n) in place; returns the total
-__device__ int block_exclusive_scan(int *buf, int n, int *warp_tot) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int carry = 0;
-  for (int base = 0; base < n; base += ES_THREADS) {
-    int i = base + tid;
-    int v = i < n ? buf[i] : 0;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_tot[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      int t = lane < ES_WARPS ? warp_tot[lane] : 0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
-      }
-      if (lane < ES_WARPS) warp_tot[lane] = t;
-    }
-    __syncthreads();
-    int off = (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
-    if (i < n) buf[i] = off + x - v;
-    int tot = warp_tot[ES_WARPS - 1];
-    __syncthreads();
-    carry += tot;
-  }
-  return carry;
-}
-
 template <int NL, int PREC>
-__device__ void solve_limb_point(const EsParams &P, cd w0, double th, cd *zrow, const cd *warm, uint16_t &mkb,
-                                 uint16_t &pp, uint16_t &zp, uint32_t &flags) {
-  constexpr int DEG = NL * NL + 1;
-  double s, c;
-  sincos(th, &s, &c);
-  cd w = mk(w0.x + P.rho * c, w0.y + P.rho * s);
-  cd p[DEG + 1], z[DEG];
-  lens_poly<NL>(P.L, w, p);
-  if (warm) {
-#pragma unroll
-    for (int i = 0; i < DEG; ++i) z[i] = warm[i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
-  }
-  int it = (PREC == MIXED) ? aberth_mixed<DEG>(p, z, P.itmax, warm != nullptr, flags)
-                           : aberth64<DEG>(p, z, P.itmax, warm != nullptr);
-  if (it < 0) flags |= CGB_ST_NOCONV;
-  mkb = 0;
-  pp = 0;
-  zp = 0;
-#pragma unroll
-  for (int i = 0; i < DEG; ++i) {
-    zrow[i] = z[i];
-    double r = cabs(lens_eq<NL>(P.L, z[i]) - w);
-    if (r < 1e-6) mkb |= 1u << i;
-    if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
-    double d = lens_det<NL>(P.L, z[i]);
-    if (d > 0) pp |= 1u << i;
-    if (d == 0) zp |= 1u << i;
-  }
-}
-
-// permute the rows of one slot in place: new row t = old row perm[t]
-template <int DEG>
-__device__ void apply_rows(cd *zrow, uint16_t &mkb, uint16_t &pp, uint16_t &zp, uint64_t perm) {
-  cd tmp[DEG];
-  uint16_t m2 = 0, p2 = 0, z2 = 0;
-  for (int t = 0; t < DEG; ++t) tmp[t] = zrow[t];
-  for (int t = 0; t < DEG; ++t) {
-    int r = perm_get(perm, t);
-    zrow[t] = tmp[r];
-    m2 |= ((mkb >> r) & 1u) << t;
-    p2 |= ((pp >> r) & 1u) << t;
-    z2 |= ((zp >> r) & 1u) << t;
-  }
-  mkb = m2;
-  pp = p2;
-  zp = z2;
-}
-
-// chained greedy matching over positions [0, n) of ORD; writes PERM[k] (track -> row)
-template <int DEG>
-__device__ void chain_match(EsSmem<DEG> &S, int n) {
-  const int tid = threadIdx.x;
-  // parallel: nearest map between consecutive positions (raw rows)
-  for (int k = 1 + tid; k < n; k += ES_THREADS) {
-    bool ok;
-    uint64_t m = nearest_map<DEG>(S.Z + (size_t)S.ORD[k - 1] * DEG, S.Z + (size_t)S.ORD[k] * DEG, ok);
-    S.PERM[k] = m;
-    S.SCAN[k] = ok ? 1 : 0;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    uint64_t prev = 0;
-    for (int t = 0; t < DEG; ++t) prev = perm_set(prev, t, t);
-    S.PERM[0] = prev;
-    for (int k = 1; k < n; ++k) {
-      uint64_t cur = 0;
-      if (S.SCAN[k]) {
-        uint64_t m = S.PERM[k];
-        for (int t = 0; t < DEG; ++t) cur = perm_set(cur, t, perm_get(m, perm_get(prev, t)));
-      } else {
-        cd a[DEG];
-        const cd *za = S.Z + (size_t)S.ORD[k - 1] * DEG;
-        for (int t = 0; t < DEG; ++t) a[t] = za[perm_get(prev, t)];
-        cur = greedy_match<DEG>(a, S.Z + (size_t)S.ORD[k] * DEG);
-      }
-      S.PERM[k] = cur;
-      prev = cur;
-    }
-  }
-  __syncthreads();
-}
-
-// ---- merging helpers (single thread) ----
-template <int DEG>
-struct TrackView {
-  const EsSmem<DEG> *S;
-  __device__ cd at(int t, int k) const {
-    int slot = S->ORD[k];
-    int row = perm_get(S->PERM[k], t);
-    return S->Z[(size_t)slot * DEG + row];
-  }
-  __device__ uint32_t cp(int t, int k) const {
-    int slot = S->ORD[k];
-    return (uint32_t)(slot * DEG + perm_get(S->PERM[k], t));
-  }
-};
-
-// point i of a piece list (0 beyond the end, like the zero padding)
-template <int DEG>
-__device__ cd pieces_point(const TrackView<DEG> &V, const Piece *pc, int np, int i, int cap) {
-  if (i < 0) i += cap;  // negative index wraps (JAX/NumPy), lands in the zero padding
-  for (int q = 0; q < np; ++q) {
-    int n = pc[q].r - pc[q].l;
-    if (i < n) return V.at(pc[q].t, pc[q].dir > 0 ? pc[q].l + i : pc[q].r - 1 - i);
-    i -= n;
-  }
-  return mk(0, 0);
-}
-
-// the two points defining a segment end (extended_source.py:373-393)
-template <int DEG>
-__device__ void end_line(const TrackView<DEG> &V, const Piece *pc, int np, int tidx, bool head, int cap, cd &l0,
-                         cd &l1) {
-  if (head) {
-    cd x0 = pieces_point(V, pc, np, 0, cap), x1 = pieces_point(V, pc, np, 1, cap);
-    if (cabs(x1 - x0) > 1e-5 || tidx <= 1) {
-      l0 = x1;
-      l1 = x0;
-    } else {
-      l0 = pieces_point(V, pc, np, 2, cap);
-      l1 = x1;
-    }
-  } else {
-    cd xt = pieces_point(V, pc, np, tidx, cap), xm = pieces_point(V, pc, np, tidx - 1, cap);
-    int s0 = (cabs(xt - xm) > 1e-5 || tidx <= 1) ? tidx - 1 : tidx - 2;
-    s0 = min(max(s0, 0), cap - 2);
-    l0 = pieces_point(V, pc, np, s0, cap);
-    l1 = pieces_point(V, pc, np, s0 + 1, cap);
-  }
-}
-
-// _connection_condition (extended_source.py:324-442)
-template <int DEG>
-__device__ bool connect_ok(const TrackView<DEG> &V, const Piece *pa, int npa, int ta, int para, const Piece *pb,
-                           int npb, int tb, int parb, int ctype, int cap) {
-  bool same = (double)para * (double)parb > 0.0;
-  bool cond_par = ctype < 2 ? same : !same;
-  cd a0, a1, b0, b1;
-  bool ahead = (ctype == 1 || ctype == 2), bhead = (ctype == 0 || ctype == 2);
-  end_line(V, pa, npa, ta, ahead, cap, a0, a1);
-  end_line(V, pb, npb, tb, bhead, cap, b0, b1);
-  double dist = cabs(a1 - b1);
-  cd v1 = a1 - a0, v2 = b1 - b0;
-  double n1 = cabs(v1), n2 = cabs(v2);
-  v1 = mk(v1.x / n1, v1.y / n1);
-  v2 = mk(v2.x / n2, v2.y / n2);
-  double ang = acos(v1.x * v2.x + v1.y * v2.y);
-  bool c1 = dist < 1e-1;
-  bool c2 = (180.0 - ang * (180.0 / 3.14159265358979323846)) < 60.0;
-  bool c3 = cabs(a1 - b1) < cabs(a0 - b0);
-  return cond_par && ((c1 && c2 && c3) || dist < 1e-5);
-}
-
-template <int DEG>
-__device__ void merge_segments(EsSmem<DEG> &S, int L) {
-  MergeState &M = *S.M;
-  TrackView<DEG> V{&S};
-  const int cap = 4 * L;  // padded length of the reference's merge arrays
-  int cur[MAX_SEG], ncur = M.nseg;
-  for (int i = 0; i < ncur; ++i) cur[i] = i;
-  int maxsteps = 20;
-  for (int c = 0; c < N_CONTOURS; ++c) {
-    // stable sort by length, zero length (NaN in the reference) last
-    int tmp[MAX_SEG], nt = 0;
-    for (int i = 0; i < ncur; ++i) {
-      const Segment &s = M.seg[cur[i]];
-      if (s.alive && s.len != 0.0) {
-        int j = nt;
-        while (j > 0) {
-          const Segment &o = M.seg[tmp[j - 1]];
-          if (o.len > s.len) {
-            tmp[j] = tmp[j - 1];
-            --j;
-          } else
-            break;
-        }
-        tmp[j] = cur[i];
-        ++nt;
-      }
-    }
-    for (int i = 0; i < ncur; ++i) {
-      const Segment &s = M.seg[cur[i]];
-      if (!(s.alive && s.len != 0.0)) tmp[nt++] = cur[i];
-    }
-    // active segment
-    Piece *pa = M.pieces[c];
-    int npa = 0, ta = 0, para = 0;
-    {
-      const Segment &s = M.seg[tmp[0]];
-      if (s.alive) {
-        pa[0] = Piece{s.t, s.l, s.r, 1};
-        npa = 1;
-        ta = s.r - s.l - 1;
-        para = s.par;
-      }
-    }
-    int rest[MAX_SEG], nrest = ncur - 1;
-    for (int i = 1; i < ncur; ++i) rest[i - 1] = tmp[i];
-    for (int step = 0; step < maxsteps; ++step) {
-      bool any = false;
-      for (int i = 0; i < nrest; ++i) any |= (M.seg[rest[i]].alive != 0);
-      if (!any) continue;
-      cd ah = pieces_point(V, pa, npa, 0, cap), at = pieces_point(V, pa, npa, ta, cap);
-      // four smallest of the 4 x nrest distances, ties by flattened index
-      double bd[4];
-      int bi[4];
-      for (int q = 0; q < 4; ++q) {
-        bd[q] = INFINITY;
-        bi[q] = 1 << 30;
-      }
-      for (int ct = 0; ct < 4; ++ct)
-        for (int i = 0; i < nrest; ++i) {
-          const Segment &s = M.seg[rest[i]];
-          cd bh = mk(0, 0), bt = mk(0, 0);
-          if (s.alive) {
-            bh = V.at(s.t, s.l);
-            bt = V.at(s.t, s.r - 1);
-          }
-          cd pa_ = (ct == 0 || ct == 3) ? at : ah;
-          cd pb_ = (ct == 0 || ct == 2) ? bh : bt;
-          double d = cabs(pa_ - pb_);
-          int f = ct * nrest + i;
-          // insert into the sorted top-4 (strictly smaller, or equal with smaller index)
-          for (int q = 0; q < 4; ++q) {
-            if (d < bd[q] || (d == bd[q] && f < bi[q]) || (isnan(d) && false)) {
-              for (int u = 3; u > q; --u) {
-                bd[u] = bd[u - 1];
-                bi[u] = bi[u - 1];
-              }
-              bd[q] = d;
-              bi[q] = f;
-              break;
-            }
-          }
-        }
-      int chosen = -1, cht = 0;
-      for (int q = 0; q < 4 && chosen < 0; ++q) {
-        if (bi[q] >= (1 << 30)) continue;
-        int ct = bi[q] / nrest, i = bi[q] % nrest;
-        const Segment &s = M.seg[rest[i]];
-        Piece pb{s.t, s.l, s.r, 1};
-        int npb = s.alive ? 1 : 0, tb = s.alive ? s.r - s.l - 1 : 0, parb = s.alive ? s.par : 0;
-        if (connect_ok(V, pa, npa, ta, para, &pb, npb, tb, parb, ct, cap)) {
-          chosen = i;
-          cht = ct;
-        }
-      }
-      if (chosen < 0) continue;
-      Segment &s = M.seg[rest[chosen]];
-      if (!s.alive || npa + 1 > MAX_PIECES) {
-        M.flags |= CGB_ST_MERGE;
-        continue;
-      }
-      Piece pb{s.t, s.l, s.r, 1};
-      int nb = s.r - s.l;
-      if (cht == 0) {  // T-H: A then B
-        pa[npa++] = pb;
-      } else if (cht == 1) {  // H-T: B then A
-        for (int u = npa; u > 0; --u) pa[u] = pa[u - 1];
-        pa[0] = pb;
-        ++npa;
-        para = s.par;
-      } else if (cht == 2) {  // H-H: reversed B (parity flipped) then A
-        for (int u = npa; u > 0; --u) pa[u] = pa[u - 1];
-        pa[0] = Piece{s.t, s.l, s.r, -1};
-        ++npa;
-        para = -s.par;
-      } else {  // T-T: A then reversed B
-        pa[npa++] = Piece{s.t, s.l, s.r, -1};
-      }
-      ta = ta + nb;  // t1 + t2 + 1
-      if (ta + 1 > cap) M.flags |= CGB_ST_MERGE;
-      s.alive = 0;
-    }
-    M.npieces[c] = npa;
-    M.cpar[c] = para;
-    M.cnpts[c] = npa > 0 ? ta + 1 : 0;
-    maxsteps -= 2;
-    ncur = nrest;
-    for (int i = 0; i < nrest; ++i) cur[i] = rest[i];
-  }
-  for (int i = 0; i < ncur; ++i)
-    if (M.seg[cur[i]].alive) M.flags |= CGB_ST_MERGE;
-}
-
-// ---- Gauss-Legendre line integrals of the limb-darkened brightness ----
-__device__ __forceinline__ double brightness_b(double r) {
-  return r <= 1.0 ? 1.0 + sqrt(fmax(1.0 - r * r, 0.0)) : 1.0 - sqrt(fmax(1.0 - 1.0 / (r * r), 0.0));
-}
-__device__ __forceinline__ float brightness_bf(float r) {
-  return r <= 1.0f ? 1.0f + sqrtf(fmaxf(1.0f - r * r, 0.0f)) : 1.0f - sqrtf(fmaxf(1.0f - 1.0f / (r * r), 0.0f));
-}
-
-// split points of integrate.py:49-64
-__device__ __forceinline__ double split_point(double a, double b, double rho) {
-  double absd = fabs(b - a);
-  double sp = b > a ? b - 2 * rho : b + 2 * rho;
-  return 0.5 * absd <= 2 * rho ? a + 0.5 * absd : sp;
-}
-
-// P_i * wx_i + Q_i * wy_i summed over this warp's share of nodes (FP64 nodes)
-template <int NL>
-__device__ double ld_point_fp64(const EsParams &P, cd w0, cd zc, cd z0, double wx, double wy, int lane) {
-  const int n1 = P.n1, n2 = P.n2, nn = n1 + n2;
-  const double c0 = 3.0 / (3.0 - P.u1), u1 = P.u1, inv_rho = 1.0 / P.rho;
-  double accP = 0.0, accQ = 0.0;
-  for (int q = lane; q < 2 * nn; q += 32) {
-    const bool isQ = q >= nn;
-    const int j = isQ ? q - nn : q;
-    const int half = j < n1 ? 0 : 1;
-    const int jj = half ? j - n1 : j;
-    const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
-    const double sp = split_point(a, b, P.rho);
-    const double lo = half ? sp : a, hi = half ? b : sp;
-    const double hw = 0.5 * (hi - lo);
-    const double xn = hw * P.gl_x[half][jj] + 0.5 * (hi + lo);
-    cd zn = isQ ? mk(xn, zc.y) : mk(zc.x, xn);
-    double r = cabs(lens_eq<NL>(P.L, zn) - w0) * inv_rho;
-    double I = c0 * (u1 * brightness_b(r) + 1.0 - 2.0 * u1);
-    double v = hw * P.gl_w[half][jj] * I;
-    if (isQ)
-      accQ += v;
-    else
-      accP += v;
-  }
-  return -0.5 * accP * wx + 0.5 * accQ * wy;
-}
-
-// FP32 nodes: lens_eq(zc + d) - w0 = (lens_eq(zc) - w0) + d + sum_j eps_j conj(d) / (D_j (D_j + conj(d))),
-// D_j = conj(zc) - conj(r_j); every FP32 quantity is a difference, not an absolute position.
-template <int NL>
-__device__ double ld_point_mixed(const EsParams &P, cd w0, cd zc, cd z0, double wx, double wy, int lane) {
-  const int n1 = P.n1, n2 = P.n2, nn = n1 + n2;
-  const float c0 = (float)(3.0 / (3.0 - P.u1)), u1 = (float)P.u1;
-  const double inv_rho = 1.0 / P.rho;
-  cd uc64 = (lens_eq<NL>(P.L, zc) - w0) * inv_rho;
-  const cf uc = tof(uc64);
-  cf Dj[NL], Dj2[NL];
-  float ej[NL];
-#pragma unroll
-  for (int j = 0; j < NL; ++j) {
-    cd d = conj(zc) - conj(P.L.r[j]);
-    Dj[j] = tof(d);
-    Dj2[j] = tof(d * d);
-    ej[j] = (float)(P.L.eps[j] * inv_rho);
-  }
-  const float irf = (float)inv_rho;
-  // per-integral interval ends relative to the contour point
-  double spP = split_point(z0.y, zc.y, P.rho), spQ = split_point(z0.x, zc.x, P.rho);
-  float accP = 0.0f, accQ = 0.0f;
-  for (int q = lane; q < 2 * nn; q += 32) {
-    const bool isQ = q >= nn;
-    const int j = isQ ? q - nn : q;
-    const int half = j < n1 ? 0 : 1;
-    const int jj = half ? j - n1 : j;
-    const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y, sp = isQ ? spQ : spP;
-    const double lo = half ? sp : a, hi = half ? b : sp;
-    const float lo_r = (float)(lo - b), hi_r = (float)(hi - b);  // relative to the contour point
-    const float hw = 0.5f * (hi_r - lo_r);
-    const float d = fmaf(hw, (float)P.gl_x[half][jj], 0.5f * (hi_r + lo_r));
-    // delta = d (Q, along x) or i d (P, along y); conj(delta) = d or -i d
-    cf cdl = isQ ? mkf(d, 0.0f) : mkf(0.0f, -d);
-    cf s = isQ ? mkf(d * irf, 0.0f) : mkf(0.0f, d * irf);
-#pragma unroll
-    for (int k = 0; k < NL; ++k) {
-      cf den = cfma(Dj[k], cdl, Dj2[k]);  // D (D + conj(delta))
-      cf t = cdl * crecip(den);
-      s = s + t * ej[k];
-    }
-    s = s + uc;
-    float r = cabs(s);
-    float I = c0 * (u1 * brightness_bf(r) + 1.0f - 2.0f * u1);
-    float v = hw * (float)P.gl_w[half][jj] * I;
-    if (isQ)
-      accQ += v;
-    else
-      accP += v;
-  }
-  return -0.5 * (double)accP * wx + 0.5 * (double)accQ * wy;
-}
-
-template <int NL, int PREC>
-__global__ void __launch_bounds__(ES_THREADS, 2) es_kernel(const EsParams P, const cd *__restrict__ w0s,
-                                                        const int64_t *__restrict__ index,
-                                                        const uint8_t *__restrict__ route, int64_t npoints,
-                                                        double *__restrict__ mag, uint32_t *__restrict__ status) {
-  constexpr int DEG = NL * NL + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int warp_tot[ES_WARPS];
-  __shared__ double contour_acc[ES_WARPS][MAX_CLOSED + N_CONTOURS];
-  __shared__ cd centroid[MAX_CLOSED + N_CONTOURS];
-  __shared__ int cstart[MAX_CLOSED + N_CONTOURS + 1];
-  __shared__ int cpar[MAX_CLOSED + N_CONTOURS];
-  __shared__ uint32_t sflags;
-  __shared__ int nsel_sh;
-  const int Lcap = P.Lcap;
-  EsSmem<DEG> S;
-  {
-    unsigned char *p = smem_raw;
-    S.Z = reinterpret_cast<cd *>(p);
-    p += sizeof(cd) * (size_t)Lcap * DEG;
-    S.TH = reinterpret_cast<double *>(p);
-    p += sizeof(double) * Lcap;
-    S.KEY = reinterpret_cast<double *>(p);
-    p += sizeof(double) * Lcap;
-    S.PERM = reinterpret_cast<uint64_t *>(p);
-    p += sizeof(uint64_t) * Lcap;
-    S.M = reinterpret_cast<MergeState *>(p);
-    p += (sizeof(MergeState) + 15) / 16 * 16;
-    S.CP = reinterpret_cast<uint32_t *>(p);
-    p += sizeof(uint32_t) * (size_t)P.CPcap;
-    S.SCAN = reinterpret_cast<int *>(p);
-    p += sizeof(int) * (Lcap + 1);
-    S.MK = reinterpret_cast<uint16_t *>(p);
-    p += sizeof(uint16_t) * Lcap;
-    S.PP = reinterpret_cast<uint16_t *>(p);
-    p += sizeof(uint16_t) * Lcap;
-    S.ZP = reinterpret_cast<uint16_t *>(p);
-    p += sizeof(uint16_t) * Lcap;
-    S.ORD = reinterpret_cast<uint16_t *>(p);
-    p += sizeof(uint16_t) * Lcap;
-    S.ORD2 = reinterpret_cast<uint16_t *>(p);
-  }
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-  for (int64_t item = blockIdx.x; item < npoints; item += gridDim.x) {
-    const int64_t pi = index ? index[item] : item;
-    if (route && route[pi] == 0) continue;  // hexadecapole accepted (CTA-uniform)
-    cd w0 = w0s[pi];
-    w0.x += P.L.x_cm;
-    if (tid == 0) sflags = 0;
-    uint32_t flags = 0;
-    __syncthreads();
-
-    // ---- A: initial limb sampling (extended_source.py:100-107) ----
-    const int n0 = P.n0;
-    for (int k = tid; k < n0; k += ES_THREADS) {
-      double th = (k < n0 - 1) ? -3.14159265358979323846 + 6.28318530717958647692 * k / (n0 - 1)
-                               : 3.14159265358979323846 - 1e-8;
-      S.TH[k] = th;
-      S.ORD[k] = (uint16_t)k;
-      solve_limb_point<NL, PREC>(P, w0, th, S.Z + (size_t)k * DEG, nullptr, S.MK[k], S.PP[k], S.ZP[k], flags);
-    }
-    __syncthreads();
-    // order rows by the matching chain so refinement gaps compare continuous tracks
-    chain_match<DEG>(S, n0);
-    for (int k = tid; k < n0; k += ES_THREADS)
-      apply_rows<DEG>(S.Z + (size_t)k * DEG, S.MK[k], S.PP[k], S.ZP[k], S.PERM[k]);
-    __syncthreads();
-
-    // ---- B: refinement rounds (extended_source.py:109-135) ----
-    int Lcur = n0;
-    for (int round = 0; round < P.niter; ++round) {
-      const int ngap = Lcur - 1;
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        const int s1 = S.ORD[k], s2 = S.ORD[k + 1];
-        const cd *a = S.Z + (size_t)s1 * DEG, *b = S.Z + (size_t)s2 * DEG;
-        const uint16_t m = S.MK[s1] | S.MK[s2];
-        double g = 0.0;
-        for (int i = 0; i < DEG; ++i)
-          if ((m >> i) & 1u) g = fmax(g, cabs(b[i] - a[i]));
-        S.KEY[k] = g;
-      }
-      __syncthreads();
-      // rank: larger gap first, ties -> larger index first
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        const double g = S.KEY[k];
-        int rank = 0;
-        for (int j = 0; j < ngap; ++j) {
-          double h = S.KEY[j];
-          rank += (h > g) || (h == g && j > k);
-        }
-        S.SCAN[k] = rank < P.n_add ? 1 : 0;
-      }
-      if (tid == 0) S.SCAN[ngap] = 0;
-      __syncthreads();
-      // positions of the selected gaps -> compact list in SCAN (exclusive scan)
-      for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
-      __syncthreads();
-      int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);
-      // new slots: selected gap k -> slot Lcur + SCAN[k]
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        if (S.KEY[k] != 0.0) {
-          const int j = S.SCAN[k];
-          const int slot = Lcur + j;
-          const int sl = S.ORD[k], sr = S.ORD[k + 1];
-          const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
-          S.TH[slot] = th;
-          solve_limb_point<NL, PREC>(P, w0, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
-                                     S.PP[slot], S.ZP[slot], flags);
-          bool ok;
-          uint64_t m = nearest_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, ok);
-          if (!ok) m = greedy_match<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG);
-          apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
-        }
-      }
-      __syncthreads();
-      // insertion: old position k -> k + (#selected before k); new point after k
-      for (int k = tid; k < Lcur; k += ES_THREADS) {
-        const int before = S.SCAN[k];
-        S.ORD2[k + before] = S.ORD[k];
-        if (k < ngap && S.KEY[k] != 0.0) S.ORD2[k + before + 1] = (uint16_t)(Lcur + before);
-      }
-      __syncthreads();
-      for (int k = tid; k < Lcur + nsel; k += ES_THREADS) S.ORD[k] = S.ORD2[k];
-      Lcur += nsel;
-      __syncthreads();
-    }
-    const int L = Lcur;
-
-    // ---- C: final chained matching (extended_source.py:150-151) ----
-    chain_match<DEG>(S, L);
-
-    // ---- D: segments (extended_source.py:251-309) ----
-    TrackView<DEG> V{&S};
-    if (tid == 0) {
-      MergeState &M = *S.M;
-      M.nseg = 0;
-      M.nclosed = 0;
-      M.flags = 0;
-      M.all_closed = 1;
-      for (int c = 0; c < N_CONTOURS; ++c) {
-        M.npieces[c] = 0;
-        M.cnpts[c] = 0;
-        M.cpar[c] = 0;
-      }
-    }
-    __syncthreads();
-    // per track: closed?  (warp t handles track t)
-    for (int t = warp; t < DEG; t += ES_WARPS) {
-      bool allreal = true;
-      for (int k = lane; k < L; k += 32) {
-        int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-        allreal &= ((S.MK[slot] >> row) & 1u) != 0;
-      }
-      allreal = __all_sync(0xffffffffu, allreal);
-      if (lane == 0) {
-        bool closed = allreal && cabs(V.at(t, 0) - V.at(t, L - 1)) < 1e-5;
-        if (closed) {
-          int q = atomicAdd(&S.M->nclosed, 1);
-          S.M->closed_tracks[q] = t;
-        } else {
-          atomicAnd(&S.M->all_closed, 0);
-        }
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      MergeState &M = *S.M;
-      // closed tracks in track order
-      for (int i = 1; i < M.nclosed; ++i)
-        for (int j = i; j > 0 && M.closed_tracks[j - 1] > M.closed_tracks[j]; --j) {
-          int x = M.closed_tracks[j];
-          M.closed_tracks[j] = M.closed_tracks[j - 1];
-          M.closed_tracks[j - 1] = x;
-        }
-      if (!M.all_closed) {
-        // split open tracks (extended_source.py:156-216); parts ordered as
-        // argsort(nonempty)[::-1]: non-empty parts by descending (track, part)
-        int nseg_keep = 3 * DEG;
-        int cand = 0;
-        for (int t = DEG - 1; t >= 0; --t) {
-          bool closed = false;
-          for (int i = 0; i < M.nclosed; ++i) closed |= M.closed_tracks[i] == t;
-          int starts[10], ends[10], ns = 0, ne = 0;
-          if (!closed) {
-            auto real_at = [&](int k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              return (int)((S.MK[slot] >> row) & 1u);
-            };
-            auto par_at = [&](int k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              if (!((S.MK[slot] >> row) & 1u)) return 0;
-              if ((S.ZP[slot] >> row) & 1u) return 0;
-              return ((S.PP[slot] >> row) & 1u) ? 1 : -1;
-            };
-            for (int k = 0; k <= L; ++k) {
-              int ch, dm;
-              if (k == 0) {
-                ch = real_at(0);
-                dm = real_at(0);
-              } else if (k == L) {
-                ch = real_at(L - 1);
-                dm = real_at(L - 1) ? -1 : 0;
-              } else {
-                int r0 = real_at(k - 1), r1 = real_at(k);
-                cd z0 = r0 ? V.at(t, k - 1) : mk(0, 0), z1 = r1 ? V.at(t, k) : mk(0, 0);
-                cd dz = z1 - z0;
-                bool jump = dz.x * dz.x + dz.y * dz.y > 0.1 * 0.1;
-                dm = r1 - r0;
-                ch = jump || (par_at(k) - par_at(k - 1) != 0) || (dm != 0);
-              }
-              if (ch && dm >= 0 && ns < 10) starts[ns++] = k;
-              if (ch && dm <= 0 && ne < 10) ends[ne++] = k;
-            }
-          }
-          for (int q = 9; q >= 0; --q) {
-            int l = q < ns ? starts[q] : 0, r = q < ne ? ends[q] : 0;
-            if (l == 0 && r == 0) continue;
-            int cnt = 0;
-            for (int k = l; k < r; ++k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              if ((S.MK[slot] >> row) & 1u) {
-                cd zz = S.Z[(size_t)slot * DEG + row];
-                cnt += (zz.x != 0.0 || zz.y != 0.0);
-              }
-            }
-            if (cnt < 2) continue;
-            if (cand < nseg_keep) {
-              Segment &s = M.seg[cand];
-              s.t = (int16_t)t;
-              s.l = (int16_t)l;
-              s.r = (int16_t)r;
-              int slot = S.ORD[l], row = perm_get(S.PERM[l], t);
-              s.par = ((S.ZP[slot] >> row) & 1u) ? 0 : (((S.PP[slot] >> row) & 1u) ? 1 : -1);
-              s.alive = 1;
-              double len = 0.0;
-              for (int k = l; k + 1 < r; ++k) len += cabs(V.at(t, k + 1) - V.at(t, k));
-              s.len = len;
-            }
-            ++cand;
-          }
-        }
-        if (cand > nseg_keep) M.flags |= CGB_ST_MERGE;
-        int nfill = min(cand, nseg_keep);
-        for (int i = nfill; i < nseg_keep; ++i) {
-          M.seg[i] = Segment{0, 0, 0, 0, 0.0, 0};
-        }
-        M.nseg = nseg_keep;
-        merge_segments<DEG>(S, L);
-      }
-    }
-    __syncthreads();
-
-    // ---- E: contour point lists ----
-    if (tid == 0) {
-      MergeState &M = *S.M;
-      int n = 0, c = 0;
-      for (int i = 0; i < M.nclosed; ++i) {
-        int t = M.closed_tracks[i];
-        cstart[c] = n;
-        int slot = S.ORD[0], row = perm_get(S.PERM[0], t);
-        cpar[c] = ((S.ZP[slot] >> row) & 1u) ? 0 : (((S.PP[slot] >> row) & 1u) ? 1 : -1);
-        n += L + 1;
-        ++c;
-      }
-      for (int k = 0; k < N_CONTOURS; ++k) {
-        if (M.cnpts[k] == 0) continue;
-        cstart[c] = n;
-        cpar[c] = M.cpar[k];
-        int np = M.cnpts[k];
-        int cap = 4 * L;
-        n += (np + 1 <= cap) ? np + 1 : np;  // closing point unless the buffer is full
-        ++c;
-      }
-      cstart[c] = n;
-      nsel_sh = c;
-      if (n > P.CPcap) M.flags |= CGB_ST_CAPACITY;
-    }
-    __syncthreads();
-    const int ncont = nsel_sh;
-    // fill CP in parallel: closed tracks
-    {
-      MergeState &M = *S.M;
-      for (int i = 0; i < M.nclosed; ++i) {
-        int t = M.closed_tracks[i];
-        int base = cstart[i];
-        for (int k = tid; k <= L; k += ES_THREADS) {
-          int kk = k < L ? k : 0;
-          if (base + k < P.CPcap) S.CP[base + k] = V.cp(t, kk);
-        }
-      }
-      if (tid == 0) {
-        int c = M.nclosed;
-        for (int k = 0; k < N_CONTOURS; ++k) {
-          if (M.cnpts[k] == 0) continue;
-          int base = cstart[c], n = cstart[c + 1] - base, i = 0;
-          for (int q = 0; q < M.npieces[k] && i < n; ++q) {
-            const Piece &pc = M.pieces[k][q];
-            for (int u = 0; u < pc.r - pc.l && i < n; ++u, ++i) {
-              int kk = pc.dir > 0 ? pc.l + u : pc.r - 1 - u;
-              if (base + i < P.CPcap) S.CP[base + i] = V.cp(pc.t, kk);
-            }
-          }
-          if (i < n && base + i < P.CPcap) S.CP[base + i] = S.CP[base];  // closing point
-          ++c;
-        }
-      }
-    }
-    __syncthreads();
-    const int ntot = min(cstart[ncont], P.CPcap);
-
-    // ---- F: integrals ----
-    for (int c = tid; c < MAX_CLOSED + N_CONTOURS; c += ES_THREADS)
-      for (int w = 0; w < ES_WARPS; ++w) contour_acc[w][c] = 0.0;
-    if (P.ld) {
-      // centroids (sum over all points incl. the closing point) / count
-      for (int c = warp; c < ncont; c += ES_WARPS) {
-        cd s = mk(0, 0);
-        int b = cstart[c], e = min(cstart[c + 1], ntot);
-        for (int i = b + lane; i < e; i += 32) s = s + S.Z[S.CP[i]];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
-          s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
-        }
-        if (lane == 0) centroid[c] = mk(s.x / (e - b), s.y / (e - b));
-      }
-    }
-    __syncthreads();
-    if (P.ld) {
-      // one warp per contour point: I_c = sum_i P_i wx_i + Q_i wy_i with trapezoid weights
-      int c = 0;
-      for (int i = warp; i < ntot; i += ES_WARPS) {
-        while (i >= cstart[c + 1]) ++c;
-        const int b = cstart[c], e = min(cstart[c + 1], ntot);
-        cd zc = S.Z[S.CP[i]];
-        cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
-        double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
-        double v = (PREC == MIXED) ? ld_point_mixed<NL>(P, w0, zc, centroid[c], wx, wy, lane)
-                                   : ld_point_fp64<NL>(P, w0, zc, centroid[c], wx, wy, lane);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) contour_acc[warp][c] += v;
-      }
-    } else {
-      // uniform: 1/2 sum (x_i + x_{i+1})/2 (y_{i+1} - y_i) - (y_i + y_{i+1})/2 (x_{i+1} - x_i)
-      int c = 0;
-      for (int i = tid; i < ntot; i += ES_THREADS) {
-        while (i >= cstart[c + 1]) ++c;
-        const int e = min(cstart[c + 1], ntot);
-        if (i + 1 >= e) continue;
-        cd a = S.Z[S.CP[i]], bq = S.Z[S.CP[i + 1]];
-        double v = 0.25 * ((a.x + bq.x) * (bq.y - a.y) - (a.y + bq.y) * (bq.x - a.x));
-        atomicAdd(&contour_acc[warp][c], v);
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double tot = 0.0;
-      double *dbg = P.dbg ? P.dbg + (size_t)pi * ES_DBG_STRIDE(P.Lcap) : nullptr;
-      for (int c = 0; c < ncont; ++c) {
-        double s = 0.0;
-        for (int w = 0; w < ES_WARPS; ++w) s += contour_acc[w][c];
-        tot += s * cpar[c];
-        if (dbg && c < 13) {
-          dbg[3 + 4 * c] = cstart[c];
-          dbg[4 + 4 * c] = cstart[c + 1] - cstart[c];
-          dbg[5 + 4 * c] = cpar[c];
-          dbg[6 + 4 * c] = s;
-        }
-      }
-      if (dbg) {
-        dbg[0] = L;
-        dbg[1] = ncont;
-        dbg[2] = S.M->flags;
-      }
-      mag[pi] = fabs(tot) / (3.14159265358979323846 * P.rho * P.rho);
-      atomicOr(&sflags, S.M->flags);
-    }
-    atomicOr(&sflags, flags);
-    __syncthreads();
-    if (tid == 0 && status) status[pi] = route ? (status[pi] | sflags) : sflags;
-    if (P.dbg)
-      for (int k = tid; k < L; k += ES_THREADS) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + k] = S.TH[S.ORD[k]];
-    __syncthreads();
-  }
-}
-
-template <int NL, int PREC>
-static cudaError_t launch_es_t(const EsParams &P, const cd *w0, const int64_t *index, const uint8_t *route,
-                               int64_t n, double *mag, uint32_t *status, int grid, cudaStream_t stream) {
-  size_t smem = es_smem_bytes(P, NL);
-  auto k = es_kernel<NL, PREC>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k<<<grid, ES_THREADS, smem, stream>>>(P, w0, index, route, n, mag, status);
-  return cudaGetLastError();
-}
+cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *index, const uint8_t *route, int64_t n,
+                              double *mag, uint32_t *status, int grid, cudaStream_t stream);
+extern template cudaError_t launch_es_variant<2, FP64>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+                                                       int64_t, double *, uint32_t *, int, cudaStream_t);
+extern template cudaError_t launch_es_variant<2, MIXED>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+                                                        int64_t, double *, uint32_t *, int, cudaStream_t);
+extern template cudaError_t launch_es_variant<3, FP64>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+                                                       int64_t, double *, uint32_t *, int, cudaStream_t);
+extern template cudaError_t launch_es_variant<3, MIXED>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+                                                        int64_t, double *, uint32_t *, int, cudaStream_t);
 
 static cudaError_t dispatch_es(const EsParams &P, const double *w0, const int64_t *index, const uint8_t *route,
                                int64_t n, double *mag, uint32_t *status, int precision, int grid,
                                cudaStream_t stream) {
-  if (n == 0) return cudaSuccess;
+  if (n == 0 && !P.qhead) return cudaSuccess;
   const cd *w = reinterpret_cast<const cd *>(w0);
-  if (P.L.n == 2)
-    return precision == MIXED ? launch_es_t<2, MIXED>(P, w, index, route, n, mag, status, grid, stream)
-                              : launch_es_t<2, FP64>(P, w, index, route, n, mag, status, grid, stream);
-  if (P.L.n == 3)
-    return precision == MIXED ? launch_es_t<3, MIXED>(P, w, index, route, n, mag, status, grid, stream)
-                              : launch_es_t<3, FP64>(P, w, index, route, n, mag, status, grid, stream);
+  const int nl = P.curves ? 2 : P.L.n;
+  if (nl == 2)
+    return precision == MIXED ? launch_es_variant<2, MIXED>(P, w, index, route, n, mag, status, grid, stream)
+                              : launch_es_variant<2, FP64>(P, w, index, route, n, mag, status, grid, stream);
+  if (nl == 3)
+    return precision == MIXED ? launch_es_variant<3, MIXED>(P, w, index, route, n, mag, status, grid, stream)
+                              : launch_es_variant<3, FP64>(P, w, index, route, n, mag, status, grid, stream);
   return cudaErrorInvalidValue;
 }
 
@@ -970,7 +50,7 @@ size_t es_smem_bytes(const EsParams &P, int nl) {
   size_t b = 0;
   b += sizeof(cd) * (size_t)P.Lcap * deg;
   b += sizeof(double) * P.Lcap * 2;
-  b += sizeof(uint64_t) * P.Lcap;
+  b += sizeof(uint64_t) * P.Lcap * 3;
   b += (sizeof(MergeState) + 15) / 16 * 16;
   b += sizeof(uint32_t) * (size_t)P.CPcap;
   b += sizeof(int) * (P.Lcap + 1);

@@ -24,8 +24,8 @@ struct Lens {
   cd N[3];        // sum_j eps_j prod_{k!=j} (z - r_k), low -> high
 };
 
-// Host-side construction from the reference's user parameters.
-inline Lens make_lens(int nlenses, double s, double q, double q3, double r3, double psi) {
+// Construction from the reference's user parameters (host or device).
+__host__ __device__ inline Lens make_lens(int nlenses, double s, double q, double q3, double r3, double psi) {
   Lens L{};
   L.n = nlenses;
   double a = 0.5 * s;

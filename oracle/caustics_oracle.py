@@ -249,9 +249,14 @@ def _lens_from_params(nlenses, params):
 
 
 def _jitter(shape, scale, salt):
-    # deterministic stand-in for the reference's PRNGKey(0) jitter (extended_source.py:83-85)
-    rng = np.random.default_rng(1234 + salt)
-    return rng.uniform(-scale, scale, shape) + 1j * rng.uniform(-scale, scale, shape)
+    """Deterministic stand-in for the reference's PRNGKey(0) draws
+    (extended_source.py:83-85, 146): root t of every warm start is moved by
+    (+-scale/2, +-scale/2), signs from bits 0 and 1 of t; the CUDA kernels use
+    the same pattern."""
+    t = np.arange(shape[-1])
+    re = np.where(t & 1, 0.5, -0.5) * scale
+    im = np.where(t & 2, 0.5, -0.5) * scale
+    return np.broadcast_to(re + 1j * im, shape)
 
 
 def match_points(a, b):

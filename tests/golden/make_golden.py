@@ -10,8 +10,10 @@ Only the container that holds the reference checkout can run this script; the
 fixtures it writes are committed and are all that the tests read.
 
 Known deviations of this harness from the reference under real JAX:
-* random jitter (extended_source.py:79-98, :144-148) uses a NumPy generator,
-  not JAX's threefry stream;
+* the warm-start jitter of the refinement solves (extended_source.py:79-98) is
+  a documented fixed +-0.5e-6 pattern (tests/golden/jaxshim/jax/random.py), not
+  JAX's threefry stream, which cannot be reproduced here; the oracle and the
+  kernels use the same pattern;
 * roots come from the reference's C++ solver through ctypes instead of an XLA
   custom call (identical code, compiled with g++ -O2 -DNDEBUG).
 

@@ -139,12 +139,14 @@ def test_limb_images(G):
 
 @pytest.mark.parametrize("k", range(6))
 def test_mag_extended_source(G, k):
-    """Relative 1e-4: the reference's own result moves by ~3e-5 when only the
-    warm-start jitter seed changes (near-tied refinement gaps)."""
+    """The fixtures and the oracle perturb warm starts with the same fixed
+    pattern; with it the restatement reproduces the reference to ~1e-12.  (With
+    a different perturbation the reference's own result moves by ~3e-5: near-tied
+    refinement gaps and ambiguous warm starts pick other midpoints.)"""
     d = G(f"mag_es{k}")
     m = np.array([O.mag_extended_source(w, float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=bool(d["ld"]),
                                         u1=float(d["u1"]), s=float(d["s"]), q=float(d["q"])) for w in d["w"]])
-    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
 
 
 def test_mag_extended_source_triple(G):
@@ -152,7 +154,7 @@ def test_mag_extended_source_triple(G):
     m = np.array([O.mag_extended_source(w, float(d["rho"]), nlenses=3, npts_limb=int(d["npts_limb"]), s=float(d["s"]),
                                         q=float(d["q"]), q3=float(d["q3"]), r3=float(d["r3"]), psi=float(d["psi"]))
                   for w in d["w"]])
-    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
 
 
 @pytest.mark.parametrize("name", ["mag_lc_cfg2", "mag_lc_q0.3"])
@@ -160,7 +162,7 @@ def test_mag_light_curve(G, name):
     d = G(name)
     m = O.mag(d["w"], float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=True, u1=float(d["u1"]),
               npts_ld=int(d["npts_ld"]), s=float(d["s"]), q=float(d["q"]))
-    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-4
+    assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
 
 
 def test_critical_curves_as_sets(G):
