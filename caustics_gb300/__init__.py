@@ -4,7 +4,11 @@ extended-source (contour-integration) magnification, hexadecapole routing —
 behind a C ABI (include/caustics_gb300.h) with the reference's Python
 signatures."""
 from .api import (  # noqa: F401
+    LightCurveMagnification,
     ehrlich_aberth,
+    mag_extended_source_grad,
+    mag_lc_batched,
+    mag_lc_batched_vjp,
     lens_eq,
     lens_eq_det_jac,
     mag,
@@ -14,4 +18,4 @@ from .api import (  # noqa: F401
 )
 
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
-           "mag"]
+           "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification"]

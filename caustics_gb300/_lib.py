@@ -35,7 +35,11 @@ class LensParams(ctypes.Structure):
 class EsOptions(ctypes.Structure):
     _fields_ = [("npts_limb", ctypes.c_int32), ("limb_darkening", ctypes.c_int32), ("u1", ctypes.c_double),
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("grid", ctypes.c_int32)]
+                ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32)]
+
+
+class CurveParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("s", "q", "rho", "u1", "u0", "alpha", "t0", "tE")]
 
 
 # name -> (restype, argtypes); every symbol the public header declares
@@ -52,9 +56,16 @@ SIGNATURES = {
                                                ctypes.POINTER(EsOptions), _P, _P]),
     "cgb_mag": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, LensParams, ctypes.POINTER(EsOptions),
                                _P, _P]),
+    "cgb_mag_extended_source_grad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
+                                                    ctypes.POINTER(EsOptions), _P, _P]),
     "cgb_debug_extended_source": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
                                                  ctypes.POINTER(EsOptions), _P, _P, _P]),
     "cgb_debug_record_len": (ctypes.c_int64, [ctypes.c_int32]),
+    "cgb_mag_lc_batched_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+    "cgb_mag_lc_batched": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
+                                          ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
+    "cgb_mag_lc_batched_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P,
+                                              ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
     "cgb_probe_fma": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
 }
 

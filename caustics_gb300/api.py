@@ -225,3 +225,110 @@ def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, n
     if return_status:
         res.append(_out(st.reshape(shape), was_np))
     return res[0] if len(res) == 1 else tuple(res)
+
+
+# ---------------------------------------------------------------------------
+# batched light curves and their vector-Jacobian product
+# ---------------------------------------------------------------------------
+
+CURVE_FIELDS = ("s", "q", "rho", "u1", "u0", "alpha", "t0", "tE")
+
+
+def _batched_args(offsets, t, curves):
+    off, _ = _to_device(offsets, torch.int64)
+    tt, _ = _to_device(t, torch.float64)
+    cv, _ = _to_device(curves, torch.float64)
+    if cv.ndim != 2 or cv.shape[1] != 8:
+        raise ValueError("curves must have shape [ncurves, 8]: " + ", ".join(CURVE_FIELDS))
+    if off.numel() != cv.shape[0] + 1:
+        raise ValueError("offsets must have ncurves + 1 entries")
+    return off.contiguous(), tt.contiguous(), cv.contiguous()
+
+
+def _workspace(n, device):
+    nbytes = int(L.lib().cgb_mag_lc_batched_workspace_bytes(n))
+    return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device), nbytes
+
+
+def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
+                   precision="mixed", grid=0, queue_chunk=1, return_route=False, return_status=False):
+    """mag() for many binary-lens light curves of uneven lengths in one pass.
+
+    offsets: int64 [ncurves+1]; t: float64 [npoints]; curves: float64
+    [ncurves, 8] = (s, q, rho, u1, u0, alpha, t0, tE) per curve, the source on
+    the rectilinear trajectory.  Per-curve u1 is used when limb_darkening."""
+    off, tt, cv = _batched_args(offsets, t, curves)
+    n = tt.numel()
+    dev = tt.device
+    mag_out = torch.empty(n, dtype=torch.float64, device=dev)
+    route = torch.empty(n, dtype=torch.uint8, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    ws, nbytes = _workspace(n, dev)
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid)
+    opts.queue_chunk = int(queue_chunk)
+    with torch.cuda.device(dev):
+        L.check(L.lib().cgb_mag_lc_batched(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
+                                           _ptr(st), opts, _ptr(ws), nbytes, _stream()), "cgb_mag_lc_batched")
+    res = [mag_out]
+    if return_route:
+        res.append(route.bool())
+    if return_status:
+        res.append(st)
+    return res[0] if len(res) == 1 else tuple(res)
+
+
+def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
+                       precision="mixed", grid=0, queue_chunk=1):
+    """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c]."""
+    off, tt, cv = _batched_args(offsets, t, curves)
+    ct, _ = _to_device(cot, torch.float64)
+    n = tt.numel()
+    dev = tt.device
+    mag_out = torch.empty(n, dtype=torch.float64, device=dev)
+    route = torch.empty(n, dtype=torch.uint8, device=dev)
+    grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
+    ws, nbytes = _workspace(n, dev)
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid)
+    opts.queue_chunk = int(queue_chunk)
+    with torch.cuda.device(dev):
+        L.check(L.lib().cgb_mag_lc_batched_vjp(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
+                                               _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
+                                               _stream()), "cgb_mag_lc_batched_vjp")
+    return grad, mag_out
+
+
+class LightCurveMagnification(torch.autograd.Function):
+    """mag of batched light curves with the hand-written adjoint as backward:
+    LightCurveMagnification.apply(curves [ncurves, 8], offsets, t, options dict)."""
+
+    @staticmethod
+    def forward(ctx, curves, offsets, t, options):
+        ctx.save_for_backward(curves, offsets, t)
+        ctx.options = dict(options)
+        return mag_lc_batched(offsets, t, curves.detach(), **ctx.options)
+
+    @staticmethod
+    def backward(ctx, gmag):
+        curves, offsets, t = ctx.saved_tensors
+        grad, _ = mag_lc_batched_vjp(offsets, t, curves.detach(), gmag.contiguous(), **ctx.options)
+        return grad.to(curves.dtype), None, None, None
+
+
+def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
+                             roots_itmax=2500, precision=None, grid=0, **params):
+    """(mag [n], grad [n, 6]) with grad = d mag / d(s, q, rho, u1, Re w0, Im w0)
+    (binary lenses): the hand-written adjoint of mag_extended_source."""
+    if nlenses != 2:
+        raise ValueError("the adjoint supports binary lenses")
+    wt, was_np = _to_device(np.atleast_1d(w0) if np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor) else w0,
+                            torch.complex128)
+    wf = wt.reshape(-1).contiguous()
+    n = wf.numel()
+    mag_out = torch.empty(n, dtype=torch.float64, device=wf.device)
+    g = torch.empty((n, 6), dtype=torch.float64, device=wf.device)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    with torch.cuda.device(wf.device):
+        L.check(L.lib().cgb_mag_extended_source_grad(_ptr(wf), _ptr(mag_out), _ptr(g), n, float(rho),
+                                                     L.lens_params(nlenses, params), opts, None, _stream()),
+                "cgb_mag_extended_source_grad")
+    return _out(mag_out, was_np), _out(g, was_np)

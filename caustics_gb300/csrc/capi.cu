@@ -114,7 +114,7 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
     gauss_legendre(P.n2, P.gl_x[1], P.gl_w[1]);
   }
   if (P.Lcap > 4096) return fail(CGB_ERR_UNSUPPORTED, "npts_limb too large (limb buffer > 4096 points)%s");
-  size_t smem = es_smem_bytes(P, lens.nlenses);
+  size_t smem = es_smem_bytes(P, lens.nlenses, lens.nlenses == 2);
   int dev = 0, maxsmem = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -192,6 +192,92 @@ int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho
   if (grid < 1) grid = 1;
   return cuda_status(launch_es(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),
                      "cgb_mag_extended_source launch");
+}
+
+int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                 cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status, void *stream) {
+  if (n < 0 || (n > 0 && (!w0 || !mag || !grad))) return fail(CGB_ERR_INVALID, "invalid buffers%s");
+  if (lens.nlenses != 2) return fail(CGB_ERR_UNSUPPORTED, "the adjoint supports binary lenses%s");
+  EsParams P;
+  int rc = make_es_params(lens, rho, opts, P);
+  if (rc) return rc;
+  P.gout = grad;
+  P.s_user = lens.s;
+  P.q_user = lens.q;
+  int grid = opts->grid > 0 ? opts->grid : (int)((n < 4 * sm_count()) ? n : 4 * sm_count());
+  if (grid < 1) grid = 1;
+  return cuda_status(launch_es_grad(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),
+                     "cgb_mag_extended_source_grad launch");
+}
+
+size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints) {
+  return 16 + 8 * (size_t)(npoints > 0 ? npoints : 0);
+}
+
+static int batched_setup(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
+                         int64_t npoints, const cgb_es_options *opts, void *ws, size_t ws_bytes, EsParams &P) {
+  if (ncurves < 1 || npoints < 0) return fail(CGB_ERR_INVALID, "need ncurves >= 1 and npoints >= 0%s");
+  if (!offsets || !curves || (npoints > 0 && !t)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!ws || ws_bytes < cgb_mag_lc_batched_workspace_bytes(npoints))
+    return fail(CGB_ERR_INVALID, "workspace too small (see cgb_mag_lc_batched_workspace_bytes)%s");
+  cgb_lens_params dummy{2, 1.0, 1.0, 0.0, 0.0, 0.0};
+  int rc = make_es_params(dummy, 1.0, opts, P);
+  if (rc) return rc;
+  P.curves = reinterpret_cast<const CurveDev *>(curves);
+  P.offsets = offsets;
+  P.times = t;
+  P.ncurves = ncurves;
+  P.qcount = reinterpret_cast<const int64_t *>(ws);
+  P.qhead = reinterpret_cast<unsigned long long *>((char *)ws + 8);
+  P.qlist = reinterpret_cast<const int64_t *>((char *)ws + 16);
+  P.qchunk = opts->queue_chunk > 0 ? opts->queue_chunk : 1;
+  return CGB_OK;
+}
+
+int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
+                       int64_t npoints, double *mag, uint8_t *route, uint32_t *status, const cgb_es_options *opts,
+                       void *workspace, size_t workspace_bytes, void *stream) {
+  if (npoints > 0 && (!mag || !route)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  EsParams P;
+  int rc = batched_setup(offsets, t, curves, ncurves, npoints, opts, workspace, workspace_bytes, P);
+  if (rc) return rc;
+  if (npoints == 0) return CGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = cuda_status(cudaMemsetAsync(workspace, 0, 16, s), "queue reset");
+  if (rc) return rc;
+  const int prec_ps = opts->precision == CGB_PREC_MIXED ? MIXED : FP64;
+  rc = cuda_status(launch_lc_points_batched(P, npoints, mag, route, status, prec_ps,
+                                            (unsigned long long *)workspace, (int64_t *)((char *)workspace + 16), false,
+                                            s),
+                   "cgb_mag_lc_batched point pass");
+  if (rc) return rc;
+  return cuda_status(launch_es_routed(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
+                     "cgb_mag_lc_batched contour pass");
+}
+
+int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
+                           int64_t npoints, const double *cot, double *grad, double *mag, uint8_t *route,
+                           uint32_t *status, const cgb_es_options *opts, void *workspace, size_t workspace_bytes,
+                           void *stream) {
+  if (!grad || (npoints > 0 && (!mag || !route || !cot))) return fail(CGB_ERR_INVALID, "null buffer%s");
+  EsParams P;
+  int rc = batched_setup(offsets, t, curves, ncurves, npoints, opts, workspace, workspace_bytes, P);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = cuda_status(cudaMemsetAsync(grad, 0, sizeof(double) * 8 * (size_t)ncurves, s), "gradient reset");
+  if (rc || npoints == 0) return rc;
+  rc = cuda_status(cudaMemsetAsync(workspace, 0, 16, s), "queue reset");
+  if (rc) return rc;
+  P.cot = cot;
+  P.cgrad = grad;
+  const int prec_ps = opts->precision == CGB_PREC_MIXED ? MIXED : FP64;
+  rc = cuda_status(launch_lc_points_batched(P, npoints, mag, route, status, prec_ps,
+                                            (unsigned long long *)workspace, (int64_t *)((char *)workspace + 16), true,
+                                            s),
+                   "cgb_mag_lc_batched_vjp point pass");
+  if (rc) return rc;
+  return cuda_status(launch_es_grad(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
+                     "cgb_mag_lc_batched_vjp contour pass");
 }
 
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,

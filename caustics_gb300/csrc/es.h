@@ -18,7 +18,10 @@ struct CurveDev {
 struct EsItem {
   Lens L;
   double rho, u1;
-  cd w0;  // source centre, shifted by x_cm
+  cd w0;          // source centre, shifted by x_cm
+  double s, q;    // the user's lens parameters (for the adjoint's chain rule)
+  int64_t curve;  // batched light curves: curve of the point, else -1
+  double tau;     // (t - t0) / tE of the point (batched)
 };
 
 struct EsParams {
@@ -44,6 +47,13 @@ struct EsParams {
   const int64_t *qcount;      // number of queued items
   const int64_t *qlist;       // queued point indices
   int qchunk;                 // items taken per grab
+  // adjoint (GRAD kernels): per-point gradient rows [n][6] of
+  // (s, q, rho, u1, Re w, Im w), or for batched light curves the cotangent
+  // weighted sum per curve [ncurves][8] of (s, q, rho, u1, u0, alpha, t0, tE)
+  double *gout;
+  const double *cot;
+  double *cgrad;
+  double s_user, q_user;  // single-lens parameters (for the adjoint's chain rule)
   double *dbg;  // optional per-point diagnostics (cgb_debug_extended_source), stride ES_DBG_STRIDE(Lcap)
   double gl_x[2][GL_MAX], gl_w[2][GL_MAX];
 };
@@ -54,7 +64,11 @@ struct EsParams {
 #define ES_DBG_HEAD (ES_DBG_CLK + 8)
 #define ES_DBG_STRIDE(lcap) (ES_DBG_HEAD + (lcap))
 
-size_t es_smem_bytes(const EsParams &P, int nl);
+size_t es_smem_bytes(const EsParams &P, int nl, bool grad = false);
+
+// adjoint of the extended-source magnification (binary lenses)
+cudaError_t launch_es_grad(const EsParams &P, const double *w0, const uint8_t *route, int64_t n, double *mag,
+                           uint32_t *status, int precision, int grid, cudaStream_t stream);
 
 cudaError_t launch_es(const EsParams &P, const double *w0, const int64_t *index, int64_t n, double *mag,
                       uint32_t *status, int precision, int grid, cudaStream_t stream);
@@ -62,6 +76,13 @@ cudaError_t launch_es(const EsParams &P, const double *w0, const int64_t *index,
 // Only the points with route[i] != 0 are integrated; status is OR-ed in.
 cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t *route, int64_t n, double *mag,
                              uint32_t *status, int precision, int grid, cudaStream_t stream);
+
+// Per-point pass of batched light curves; routed points are appended to the
+// device queue (qcount, qlist).  grad: hexadecapole-routed points add their
+// cotangent-weighted gradient to P.cgrad.
+cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
+                                     int precision, unsigned long long *qcount, int64_t *qlist, bool grad,
+                                     cudaStream_t stream);
 
 // Gauss-Legendre nodes/weights on [-1, 1], ascending (host)
 void gauss_legendre(int n, double *x, double *w);

@@ -70,6 +70,9 @@ struct EsSmem {
   uint64_t *PERM; // [Lcap] packed 4-bit permutation: track -> row
   uint64_t *BMAP; // [Lcap] warm-start map of the limb chain: root of k-1 -> root of k
   uint64_t *USED; // [Lcap] chain order of k-1 the map was computed with
+  uint64_t *CAND; // [Lcap * DEG] candidate rows of position k sorted by distance, per row of k-1
+  cd *PQ;         // [CPcap] adjoint: (P_i, Q_i) per contour point
+  cd *GG;         // [CPcap] adjoint: dT/dx_i + i dT/dy_i per contour point
   double *KEY;    // [Lcap]
   int *SCAN;      // [Lcap + 1]
   uint32_t *CP;   // [CPcap] contour points: slot * DEG + row
@@ -197,7 +200,7 @@ __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, 
 
 // Step map between consecutive limb points (raw rows of k-1 -> raw rows of k).
 // When every root of k-1 has a successor clearly nearer than any other root
-// (d1 < d2/4, and no two share one) a warm-started Aberth iteration lands each
+// (d1 < d2/2, and no two share one) a warm-started Aberth iteration lands each
 // iterate on that nearest root whatever the arithmetic, so the map is final.
 // Otherwise the step is ambiguous and the returned greedy map is only a guess.
 template <int DEG>
@@ -218,7 +221,7 @@ __device__ uint64_t step_map(const cd *a, const cd *b, bool &ambiguous) {
         d2 = d;
       }
     }
-    if (!(d1 < 0.0625 * d2) || ((used >> best) & 1u)) ambiguous = true;
+    if (!(d1 < 0.25 * d2) || ((used >> best) & 1u)) ambiguous = true;
     used |= 1u << best;
     res = perm_set(res, i, best);
   }
@@ -281,16 +284,33 @@ __device__ void apply_rows(cd *zrow, uint16_t &mkb, uint16_t &pp, uint16_t &zp, 
   zp = z2;
 }
 
-// chained greedy matching over positions [0, n) of ORD; writes PERM[k] (track -> row)
+// Chained greedy matching over positions [0, n) of ORD (utils.py:15-40 applied
+// along the limb, extended_source.py:34-53); writes PERM[k] = track -> row.
+// In parallel, every row of position k-1 gets its candidate rows of position k
+// sorted by distance (stable, 4 bits each); the sequential pass is then pure
+// integer work: each track, in track order, takes its first untaken candidate.
 template <int DEG>
 __device__ void chain_match(EsSmem<DEG> &S, int n) {
   const int tid = threadIdx.x;
-  // parallel: nearest map between consecutive positions (raw rows)
-  for (int k = 1 + tid; k < n; k += ES_THREADS) {
-    bool ok;
-    uint64_t m = nearest_map<DEG>(S.Z + (size_t)S.ORD[k - 1] * DEG, S.Z + (size_t)S.ORD[k] * DEG, ok);
-    S.PERM[k] = m;
-    S.SCAN[k] = ok ? 1 : 0;
+  for (int idx = tid; idx < (n - 1) * DEG; idx += ES_THREADS) {
+    const int k = 1 + idx / DEG, i = idx % DEG;
+    const cd a = S.Z[(size_t)S.ORD[k - 1] * DEG + i];
+    const cd *b = S.Z + (size_t)S.ORD[k] * DEG;
+    double d[DEG];
+    int o[DEG];
+    for (int j = 0; j < DEG; ++j) {
+      d[j] = norm2(b[j] - a);
+      o[j] = j;
+    }
+    for (int j = 1; j < DEG; ++j)  // stable insertion sort
+      for (int m = j; m > 0 && d[o[m]] < d[o[m - 1]]; --m) {
+        int x = o[m];
+        o[m] = o[m - 1];
+        o[m - 1] = x;
+      }
+    uint64_t packed = 0;
+    for (int j = 0; j < DEG; ++j) packed = perm_set(packed, j, o[j]);
+    S.CAND[(size_t)k * DEG + i] = packed;
   }
   __syncthreads();
   if (tid == 0) {
@@ -299,14 +319,17 @@ __device__ void chain_match(EsSmem<DEG> &S, int n) {
     S.PERM[0] = prev;
     for (int k = 1; k < n; ++k) {
       uint64_t cur = 0;
-      if (S.SCAN[k]) {
-        uint64_t m = S.PERM[k];
-        for (int t = 0; t < DEG; ++t) cur = perm_set(cur, t, perm_get(m, perm_get(prev, t)));
-      } else {
-        cd a[DEG];
-        const cd *za = S.Z + (size_t)S.ORD[k - 1] * DEG;
-        for (int t = 0; t < DEG; ++t) a[t] = za[perm_get(prev, t)];
-        cur = greedy_match<DEG>(a, S.Z + (size_t)S.ORD[k] * DEG);
+      uint32_t taken = 0;
+      for (int t = 0; t < DEG; ++t) {
+        const uint64_t cand = S.CAND[(size_t)k * DEG + perm_get(prev, t)];
+        for (int j = 0; j < DEG; ++j) {
+          const int c = perm_get(cand, j);
+          if (!((taken >> c) & 1u)) {
+            taken |= 1u << c;
+            cur = perm_set(cur, t, c);
+            break;
+          }
+        }
       }
       S.PERM[k] = cur;
       prev = cur;
@@ -533,12 +556,12 @@ __device__ __forceinline__ double split_point(double a, double b, double rho) {
   return 0.5 * absd <= 2 * rho ? a + 0.5 * absd : sp;
 }
 
-// Contribution P_i wx_i + Q_i wy_i of one contour point (one thread), where
+// (P_i, Q_i) of one contour point (one thread), where
 // P_i = -1/2 int_{y0}^{y_i} I(x_i, y) dy and Q_i = 1/2 int_{x0}^{x_i} I(x, y_i) dx,
 // each split at the reference's split point into two Gauss-Legendre pieces.
 // The node loop is uniform across the warp, so node tables are broadcast.
 template <int NL>
-__device__ double ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0, double wx, double wy) {
+__device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0) {
   const double c0 = 3.0 / (3.0 - It.u1), u1 = It.u1, inv_rho = 1.0 / It.rho;
   const cd w0 = It.w0;
   double acc[2] = {0.0, 0.0};
@@ -562,7 +585,7 @@ __device__ double ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z
       acc[isQ] += hw * sum;
     }
   }
-  return -0.5 * acc[0] * wx + 0.5 * acc[1] * wy;
+  return mk(-0.5 * acc[0], 0.5 * acc[1]);  // (P_i, Q_i)
 }
 
 // FP32 nodes on a shifted lens equation:
@@ -571,7 +594,7 @@ __device__ double ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z
 // the FP64 prologue (once per point) provides every difference, so each FP32
 // quantity is small relative to its own scale.
 template <int NL>
-__device__ double ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0, double wx, double wy) {
+__device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0) {
   const float c0 = (float)(3.0 / (3.0 - It.u1)), u1 = (float)It.u1;
   const double inv_rho = 1.0 / It.rho;
   const cf uc = tof((lens_eq<NL>(It.L, zc) - It.w0) * inv_rho);
@@ -615,11 +638,312 @@ __device__ double ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd 
       acc[isQ] += (double)hw * (double)sum;
     }
   }
-  return -0.5 * acc[0] * wx + 0.5 * acc[1] * wy;
+  return mk(-0.5 * acc[0], 0.5 * acc[1]);  // (P_i, Q_i)
 }
 
+
+// ---- adjoint of the contour integral (binary lenses) ----
+// Derivatives of one contour point's P_i / Q_i (integrate.py:49-109) with
+// respect to its own position, the contour centroid coordinate, and the
+// parameters (rho, u1, Re w0, Im w0, a, e1), differentiating through the node
+// positions, the split point and the brightness profile exactly as the
+// discretised integral depends on them.
+struct PQGrad {
+  double P, Q;
+  double Px, Py, Pa;  // dP/dx_i, dP/dy_i, dP/dy0
+  double Qx, Qy, Qa;  // dQ/dx_i, dQ/dy_i, dQ/dx0
+  double Pk[6], Qk[6];  // rho, u1, Re w0, Im w0, a, e1
+};
+
+enum { GK_RHO = 0, GK_U1 = 1, GK_WX = 2, GK_WY = 3, GK_A = 4, GK_E1 = 5 };
+
+__device__ __forceinline__ void split_point_grad(double a, double b, double rho, double &sp, double &da, double &db,
+                                                 double &drho) {
+  const double absd = fabs(b - a);
+  const double sg = b > a ? 1.0 : (b < a ? -1.0 : 0.0);
+  if (0.5 * absd <= 2 * rho) {
+    sp = a + 0.5 * absd;
+    da = 1.0 - 0.5 * sg;
+    db = 0.5 * sg;
+    drho = 0.0;
+  } else if (b > a) {
+    sp = b - 2 * rho;
+    da = 0.0;
+    db = 1.0;
+    drho = -2.0;
+  } else {
+    sp = b + 2 * rho;
+    da = 0.0;
+    db = 1.0;
+    drho = 2.0;
+  }
+}
+
+template <typename R, typename C>
+__device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad &g) {
+  // shifted lens equation around the contour point (binary: r_0 = a, r_1 = -a)
+  const double rho = It.rho, inv_rho = 1.0 / rho;
+  const cd uc64 = (lens_eq<2>(It.L, zc) - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
+  C uc = C{(R)uc64.x, (R)uc64.y};
+  C Dj[2], iDj[2];
+  R ej[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    cd d = conj(zc) - conj(It.L.r[k]);
+    cd id = crecip(d);
+    Dj[k] = C{(R)d.x, (R)d.y};
+    iDj[k] = C{(R)id.x, (R)id.y};
+    ej[k] = (R)It.L.eps[k];
+  }
+  const R irho = (R)inv_rho, u1 = (R)It.u1;
+  const R c0 = (R)(3.0 / (3.0 - It.u1)), dc0 = (R)(3.0 / ((3.0 - It.u1) * (3.0 - It.u1)));
+#pragma unroll
+  for (int isQ = 0; isQ < 2; ++isQ) {
+    const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
+    double sp, dsa, dsb, dsr;
+    split_point_grad(a, b, rho, sp, dsa, dsb, dsr);
+    double val = 0.0, fixed = 0.0, kk[6] = {0, 0, 0, 0, 0, 0}, dlo[2], dhi[2];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const double lo = half ? sp : a, hi = half ? b : sp;
+      const R lo_r = (R)(lo - b), hi_r = (R)(hi - b);
+      const R hw = (R)0.5 * (hi_r - lo_r), mid = (R)0.5 * (hi_r + lo_r);
+      const int n = half ? P.n2 : P.n1;
+      R A = 0, Bl = 0, Bh = 0, Cf = 0, Ck[6] = {0, 0, 0, 0, 0, 0};
+      for (int j = 0; j < n; ++j) {
+        const R t = (R)P.gl_x[half][j], w = (R)P.gl_w[half][j];
+        const R d = hw * t + mid;
+        const C cdl = isQ ? C{d, (R)0} : C{(R)0, -d};  // conj(delta)
+        // s/rho = uc + delta/rho + sum eps conj(delta) / (D (D + conj(delta))) / rho
+        C srho = isQ ? C{uc.x + d * irho, uc.y} : C{uc.x, uc.y + d * irho};
+        C u[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          u[k] = crecip(Dj[k] + cdl);
+          srho = srho + cdl * u[k] * iDj[k] * (ej[k] * irho);
+        }
+        const R r = cabs(srho);
+        R B, dB;
+        if (r <= (R)1) {
+          const R x = (R)1 - r * r;
+          const R sq = x > (R)0 ? sqrt(x) : (R)0;
+          B = (R)1 + sq;
+          dB = x > (R)0 ? -r / sq : (R)0;
+        } else {
+          const R x = (R)1 - (R)1 / (r * r);
+          const R sq = x > (R)0 ? sqrt(x) : (R)0;
+          B = (R)1 - sq;
+          dB = x > (R)0 ? -(R)1 / (r * r * r * sq) : (R)0;
+        }
+        const R I = c0 * (u1 * B + (R)1 - (R)2 * u1);
+        const R dIdr = c0 * u1 * dB;
+        const R dIdu1 = dc0 * (u1 * B + (R)1 - (R)2 * u1) + c0 * (B - (R)2);
+        // unit vector of s, and d r = Re(conj(shat) ds) / rho
+        const R ir = r > (R)0 ? (R)1 / r : (R)0;
+        const C sh = C{srho.x * ir, srho.y * ir};
+        const C lam = u[0] * u[0] * ej[0] + u[1] * u[1] * ej[1];
+        const C fa = u[0] * u[0] * ej[0] - u[1] * u[1] * ej[1];
+        const C fe = u[0] - u[1];
+        // d s / d x' = 1 + lam ; d s / d y' = i (1 - lam)
+        const R drx = (sh.x * ((R)1 + lam.x) + sh.y * lam.y) * irho;
+        const R dry = (sh.x * lam.y + sh.y * ((R)1 - lam.x)) * irho;
+        const R dr_along = isQ ? drx : dry, dr_fixed = isQ ? dry : drx;
+        const R Iy = dIdr * dr_along;
+        const R wI = w * I;
+        A += wI;
+        Bl += w * Iy * (R)0.5 * ((R)1 - t);
+        Bh += w * Iy * (R)0.5 * ((R)1 + t);
+        Cf += w * dIdr * dr_fixed;
+        Ck[GK_RHO] += w * dIdr * (-r * irho);
+        Ck[GK_U1] += w * dIdu1;
+        Ck[GK_WX] += w * dIdr * (-sh.x * irho);
+        Ck[GK_WY] += w * dIdr * (-sh.y * irho);
+        Ck[GK_A] += w * dIdr * (-(sh.x * fa.x + sh.y * fa.y) * irho);
+        Ck[GK_E1] += w * dIdr * (-(sh.x * fe.x + sh.y * fe.y) * irho);
+      }
+      val += (double)hw * (double)A;
+      fixed += (double)hw * (double)Cf;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) kk[k] += (double)hw * (double)Ck[k];
+      dlo[half] = -0.5 * (double)A + (double)hw * (double)Bl;
+      dhi[half] = 0.5 * (double)A + (double)hw * (double)Bh;
+    }
+    const double dsp = dhi[0] + dlo[1];
+    const double d_a = dlo[0] + dsp * dsa, d_b = dhi[1] + dsp * dsb;
+    kk[GK_RHO] += dsp * dsr;
+    const double f = isQ ? 0.5 : -0.5;
+    if (!isQ) {
+      g.P = f * val;
+      g.Py = f * d_b;
+      g.Pa = f * d_a;
+      g.Px = f * fixed;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) g.Pk[k] = f * kk[k];
+    } else {
+      g.Q = f * val;
+      g.Qx = f * d_b;
+      g.Qa = f * d_a;
+      g.Qy = f * fixed;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) g.Qk[k] = f * kk[k];
+    }
+  }
+}
+
+
+// Backward pass of one extended-source evaluation (binary lenses): the
+// contours of the forward pass are recomputed, never stored between passes.
+// T = sum_c parity_c I_c, mu = |T| / (pi rho^2).
 template <int NL, int PREC>
-__global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
+__device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsItem &I, int ncont, int ntot,
+                            const int *cstart, const int *cpar, const cd *centroid,
+                            double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2], double *pgr,
+                            double *tot_sh, int64_t pi, double *mag) {
+  constexpr int DEG = NL * NL + 1;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int c = 0; c < ncont; ++c) {
+      double s = 0.0;
+      for (int w = 0; w < ES_WARPS; ++w) s += contour_acc[w][c];
+      tot += s * cpar[c];
+    }
+    *tot_sh = tot;
+  }
+  for (int i = tid; i < ntot; i += ES_THREADS) S.GG[i] = mk(0, 0);
+  __syncthreads();
+  // pass 2: node-level derivatives, trapezoid weights, centroids, direct terms
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  {
+    int c = 0;
+    for (int i = tid; i < ntot; i += ES_THREADS) {
+      while (i >= cstart[c + 1]) ++c;
+      const int b = cstart[c], e = min(cstart[c + 1], ntot);
+      const double pc = cpar[c];
+      const int ip = i > b ? i - 1 : i, in = i + 1 < e ? i + 1 : i;
+      const cd zc = S.Z[S.CP[i]], zp = S.Z[S.CP[ip]], zn = S.Z[S.CP[in]];
+      if (P.ld) {
+        const double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
+        PQGrad g;
+        if (PREC == MIXED)
+          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g);
+        else
+          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g);
+        const cd pq = S.PQ[i];
+        atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
+        atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
+        // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2
+        atomicAdd(&S.GG[in].x, 0.5 * pc * pq.x);
+        atomicAdd(&S.GG[ip].x, -0.5 * pc * pq.x);
+        atomicAdd(&S.GG[in].y, 0.5 * pc * pq.y);
+        atomicAdd(&S.GG[ip].y, -0.5 * pc * pq.y);
+        atomicAdd(&cgr[c][1], pc * wx * g.Pa);
+        atomicAdd(&cgr[c][0], pc * wy * g.Qa);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[k] += pc * (wx * g.Pk[k] + wy * g.Qk[k]);
+      } else if (i + 1 < e) {
+        // pair (i, i+1): 1/4 [(x_i + x_{i+1})(y_{i+1} - y_i) - (y_i + y_{i+1})(x_{i+1} - x_i)]
+        const cd a = zc, q = zn;
+        atomicAdd(&S.GG[i].x, pc * 0.5 * q.y);
+        atomicAdd(&S.GG[i].y, -pc * 0.5 * q.x);
+        atomicAdd(&S.GG[i + 1].x, -pc * 0.5 * a.y);
+        atomicAdd(&S.GG[i + 1].y, pc * 0.5 * a.x);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0 && v != 0.0) atomicAdd(&pgr[k], v);
+    acc[k] = 0.0;
+  }
+  __syncthreads();
+  // pass 3: every contour point's image through the lens equation:
+  // dz + lam conj(dz) = dw0 + e^{i theta} drho + f_a da + f_e1 de1, lam = sum eps/(conj z - r)^2
+  {
+    int c = 0;
+    for (int i = tid; i < ntot; i += ES_THREADS) {
+      while (i >= cstart[c + 1]) ++c;
+      const int b = cstart[c], e = min(cstart[c + 1], ntot);
+      cd G = S.GG[i];
+      if (P.ld) {
+        const double inv_n = 1.0 / (double)(e - b);
+        G = G + mk(cgr[c][0] * inv_n, cgr[c][1] * inv_n);
+      }
+      const uint32_t cp = S.CP[i];
+      const cd z = S.Z[cp];
+      const double th = S.TH[cp / DEG];
+      const cd u0 = crecip(conj(z) - I.L.r[0]), u1 = crecip(conj(z) - I.L.r[1]);
+      const cd lam = u0 * u0 * I.L.eps[0] + u1 * u1 * I.L.eps[1];
+      const double D = 1.0 - norm2(lam);
+      const cd H = cdiv(conj(G) - G * conj(lam), mk(D, 0.0));
+      const cd fa = u0 * u0 * I.L.eps[0] - u1 * u1 * I.L.eps[1];
+      const cd fe = u0 - u1;
+      double sn, cs;
+      sincos(th, &sn, &cs);
+      acc[GK_WX] += H.x;
+      acc[GK_WY] += -H.y;
+      acc[GK_RHO] += H.x * cs - H.y * sn;
+      acc[GK_A] += H.x * fa.x - H.y * fa.y;
+      acc[GK_E1] += H.x * fe.x - H.y * fe.y;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0 && v != 0.0) atomicAdd(&pgr[k], v);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double tot = *tot_sh, rho = I.rho;
+    const double mu = fabs(tot) / (3.14159265358979323846 * rho * rho);
+    const double sT = (tot > 0 ? 1.0 : (tot < 0 ? -1.0 : 0.0)) / (3.14159265358979323846 * rho * rho);
+    double d[6];
+    for (int k = 0; k < 6; ++k) d[k] = sT * pgr[k];
+    d[GK_RHO] -= 2.0 * mu / rho;
+    // (a, e1, x_cm) -> (s, q): a = s/2, e1 = 1/(1+q), x_cm = a(1-q)/(1+q)
+    const double q = I.q, a = 0.5 * I.s, opq = 1.0 + q;
+    const double ds = 0.5 * d[GK_A] + d[GK_WX] * (1.0 - q) / (2.0 * opq);
+    const double dq = -d[GK_E1] / (opq * opq) - d[GK_WX] * 2.0 * a / (opq * opq);
+    mag[pi] = mu;
+    if (I.curve >= 0 && P.cgrad) {
+      const CurveDev cv = P.curves[I.curve];
+      const double ct = P.cot ? P.cot[pi] : 1.0;
+      double sa, ca;
+      sincos(cv.alpha, &sa, &ca);
+      const double tau = I.tau;
+      // w = (u0 cos a + tau sin a) + i (-u0 sin a + tau cos a), tau = (t - t0)/tE
+      const double du0 = d[GK_WX] * ca - d[GK_WY] * sa;
+      const double dal = d[GK_WX] * (-cv.u0 * sa + tau * ca) + d[GK_WY] * (-cv.u0 * ca - tau * sa);
+      const double dt0 = -(d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
+      const double dtE = -tau * (d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
+      double *gp = P.cgrad + I.curve * 8;
+      atomicAdd(gp + 0, ct * ds);
+      atomicAdd(gp + 1, ct * dq);
+      atomicAdd(gp + 2, ct * d[GK_RHO]);
+      atomicAdd(gp + 3, ct * d[GK_U1]);
+      atomicAdd(gp + 4, ct * du0);
+      atomicAdd(gp + 5, ct * dal);
+      atomicAdd(gp + 6, ct * dt0);
+      atomicAdd(gp + 7, ct * dtE);
+    } else if (P.gout) {
+      double *gp = P.gout + pi * 6;
+      gp[0] = ds;
+      gp[1] = dq;
+      gp[2] = d[GK_RHO];
+      gp[3] = d[GK_U1];
+      gp[4] = d[GK_WX];
+      gp[5] = d[GK_WY];
+    }
+  }
+}
+
+template <int NL, int PREC, bool GRAD = false>
+__global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                         const int64_t *__restrict__ index,
                                                         const uint8_t *__restrict__ route, int64_t npoints,
                                                         double *__restrict__ mag, uint32_t *__restrict__ status) {
@@ -635,6 +959,9 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
   __shared__ EsItem item;
+  __shared__ double cgr[MAX_CLOSED + N_CONTOURS][2];  // adjoint: dT/dx0_c, dT/dy0_c
+  __shared__ double pgr[6];                          // adjoint: direct dT/d(rho, u1, w0x, w0y, a, e1)
+  __shared__ double tot_sh;
   const int Lcap = P.Lcap;
   EsSmem<DEG> S;
   {
@@ -651,6 +978,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     p += sizeof(uint64_t) * Lcap;
     S.USED = reinterpret_cast<uint64_t *>(p);
     p += sizeof(uint64_t) * Lcap;
+    S.CAND = reinterpret_cast<uint64_t *>(p);
+    p += sizeof(uint64_t) * (size_t)Lcap * DEG;
     S.M = reinterpret_cast<MergeState *>(p);
     p += (sizeof(MergeState) + 15) / 16 * 16;
     S.CP = reinterpret_cast<uint32_t *>(p);
@@ -666,6 +995,11 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     S.ORD = reinterpret_cast<uint16_t *>(p);
     p += sizeof(uint16_t) * Lcap;
     S.ORD2 = reinterpret_cast<uint16_t *>(p);
+    p += sizeof(uint16_t) * Lcap;
+    p = smem_raw + (((size_t)(p - smem_raw) + 15) / 16 * 16);
+    S.PQ = reinterpret_cast<cd *>(p);
+    p += sizeof(cd) * (size_t)P.CPcap;
+    S.GG = reinterpret_cast<cd *>(p);
   }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -711,12 +1045,20 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         double sa, ca;
         sincos(cv.alpha, &sa, &ca);
         item.w0 = mk(cv.u0 * ca + tau * sa + item.L.x_cm, -cv.u0 * sa + tau * ca);
+        item.s = cv.s;
+        item.q = cv.q;
+        item.curve = lo;
+        item.tau = tau;
       } else {
         item.L = P.L;
         item.rho = P.rho;
         item.u1 = P.u1;
         cd w = w0s[pi];
         item.w0 = mk(w.x + P.L.x_cm, w.y);
+        item.s = P.s_user;
+        item.q = P.q_user;
+        item.curve = -1;
+        item.tau = 0.0;
       }
       sflags = 0;
     }
@@ -1037,8 +1379,11 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     if (P.dbg && tid == 0) clk[5] = clock64();
 
     // ---- F: integrals ----
-    for (int c = tid; c < MAX_CLOSED + N_CONTOURS; c += ES_THREADS)
+    for (int c = tid; c < MAX_CLOSED + N_CONTOURS; c += ES_THREADS) {
       for (int w = 0; w < ES_WARPS; ++w) contour_acc[w][c] = 0.0;
+      cgr[c][0] = cgr[c][1] = 0.0;
+    }
+    if (tid < 6) pgr[tid] = 0.0;
     if (P.ld) {
       // centroids (sum over all points incl. the closing point) / count
       for (int c = warp; c < ncont; c += ES_WARPS) {
@@ -1063,9 +1408,9 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         cd zc = S.Z[S.CP[i]];
         cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
         double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
-        double v = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, zc, centroid[c], wx, wy)
-                                   : ld_point_fp64<NL>(P, I, zc, centroid[c], wx, wy);
-        atomicAdd(&contour_acc[warp][c], v);
+        cd pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, zc, centroid[c]) : ld_point_fp64<NL>(P, I, zc, centroid[c]);
+        if (GRAD) S.PQ[i] = pq;
+        atomicAdd(&contour_acc[warp][c], pq.x * wx + pq.y * wy);
       }
     } else {
       // uniform: 1/2 sum (x_i + x_{i+1})/2 (y_{i+1} - y_i) - (y_i + y_{i+1})/2 (x_{i+1} - x_i)
@@ -1080,7 +1425,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       }
     }
     __syncthreads();
-    if (tid == 0) {
+    if (GRAD) es_backward<NL, PREC>(P, S, I, ncont, ntot, cstart, cpar, centroid, contour_acc, cgr, pgr, &tot_sh, pi, mag);
+    if (tid == 0 && !GRAD) {
       double tot = 0.0;
       double *dbg = P.dbg ? P.dbg + (size_t)pi * ES_DBG_STRIDE(P.Lcap) : nullptr;
       for (int c = 0; c < ncont; ++c) {
@@ -1102,8 +1448,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         for (int c = 1; c < 7; ++c) dbg[ES_DBG_CLK + c - 1] = (double)(clk[c] - clk[c - 1]);
       }
       mag[pi] = fabs(tot) / (3.14159265358979323846 * I.rho * I.rho);
-      atomicOr(&sflags, S.M->flags);
     }
+    if (tid == 0) atomicOr(&sflags, S.M->flags);
     atomicOr(&sflags, flags);
     __syncthreads();
     if (tid == 0 && status) status[pi] = route ? (status[pi] | sflags) : sflags;
@@ -1113,13 +1459,20 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
   }
 }
 
-template <int NL, int PREC>
+template <int NL, int PREC, bool GRAD>
 cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *index, const uint8_t *route, int64_t n,
                               double *mag, uint32_t *status, int grid, cudaStream_t stream) {
-  size_t smem = es_smem_bytes(P, NL);
-  auto k = es_kernel<NL, PREC>;
+  size_t smem = es_smem_bytes(P, NL, GRAD);
+  auto k = es_kernel<NL, PREC, GRAD>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  if (grid <= 0) {  // persistent: as many CTAs as fit on the device
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, ES_THREADS, smem);
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
   k<<<grid, ES_THREADS, smem, stream>>>(P, w0, index, route, n, mag, status);
   return cudaGetLastError();
 }

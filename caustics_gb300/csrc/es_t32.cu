@@ -2,6 +2,7 @@
 #include "es_kernel.cuh"
 
 namespace cgb {
-template cudaError_t launch_es_variant<3, MIXED>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
-                                                     int64_t, double *, uint32_t *, int, cudaStream_t);
+template cudaError_t launch_es_variant<3, MIXED, false>(const EsParams &, const cd *, const int64_t *,
+                                                          const uint8_t *, int64_t, double *, uint32_t *, int,
+                                                          cudaStream_t);
 }  // namespace cgb

@@ -8,17 +8,24 @@
 
 namespace cgb {
 
-template <int NL, int PREC>
+template <int NL, int PREC, bool GRAD>
 cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *index, const uint8_t *route, int64_t n,
                               double *mag, uint32_t *status, int grid, cudaStream_t stream);
-extern template cudaError_t launch_es_variant<2, FP64>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+extern template cudaError_t launch_es_variant<2, FP64, false>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
                                                        int64_t, double *, uint32_t *, int, cudaStream_t);
-extern template cudaError_t launch_es_variant<2, MIXED>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+extern template cudaError_t launch_es_variant<2, MIXED, false>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
                                                         int64_t, double *, uint32_t *, int, cudaStream_t);
-extern template cudaError_t launch_es_variant<3, FP64>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+extern template cudaError_t launch_es_variant<3, FP64, false>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
                                                        int64_t, double *, uint32_t *, int, cudaStream_t);
-extern template cudaError_t launch_es_variant<3, MIXED>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
+extern template cudaError_t launch_es_variant<3, MIXED, false>(const EsParams &, const cd *, const int64_t *, const uint8_t *,
                                                         int64_t, double *, uint32_t *, int, cudaStream_t);
+
+extern template cudaError_t launch_es_variant<2, FP64, true>(const EsParams &, const cd *, const int64_t *,
+                                                             const uint8_t *, int64_t, double *, uint32_t *, int,
+                                                             cudaStream_t);
+extern template cudaError_t launch_es_variant<2, MIXED, true>(const EsParams &, const cd *, const int64_t *,
+                                                              const uint8_t *, int64_t, double *, uint32_t *, int,
+                                                              cudaStream_t);
 
 static cudaError_t dispatch_es(const EsParams &P, const double *w0, const int64_t *index, const uint8_t *route,
                                int64_t n, double *mag, uint32_t *status, int precision, int grid,
@@ -27,11 +34,11 @@ static cudaError_t dispatch_es(const EsParams &P, const double *w0, const int64_
   const cd *w = reinterpret_cast<const cd *>(w0);
   const int nl = P.curves ? 2 : P.L.n;
   if (nl == 2)
-    return precision == MIXED ? launch_es_variant<2, MIXED>(P, w, index, route, n, mag, status, grid, stream)
-                              : launch_es_variant<2, FP64>(P, w, index, route, n, mag, status, grid, stream);
+    return precision == MIXED ? launch_es_variant<2, MIXED, false>(P, w, index, route, n, mag, status, grid, stream)
+                              : launch_es_variant<2, FP64, false>(P, w, index, route, n, mag, status, grid, stream);
   if (nl == 3)
-    return precision == MIXED ? launch_es_variant<3, MIXED>(P, w, index, route, n, mag, status, grid, stream)
-                              : launch_es_variant<3, FP64>(P, w, index, route, n, mag, status, grid, stream);
+    return precision == MIXED ? launch_es_variant<3, MIXED, false>(P, w, index, route, n, mag, status, grid, stream)
+                              : launch_es_variant<3, FP64, false>(P, w, index, route, n, mag, status, grid, stream);
   return cudaErrorInvalidValue;
 }
 
@@ -45,16 +52,27 @@ cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t 
   return dispatch_es(P, w0, nullptr, route, n, mag, status, precision, grid, stream);
 }
 
-size_t es_smem_bytes(const EsParams &P, int nl) {
+cudaError_t launch_es_grad(const EsParams &P, const double *w0, const uint8_t *route, int64_t n, double *mag,
+                           uint32_t *status, int precision, int grid, cudaStream_t stream) {
+  if (n == 0 && !P.qhead) return cudaSuccess;
+  if (!P.curves && P.L.n != 2) return cudaErrorInvalidValue;
+  const cd *w = reinterpret_cast<const cd *>(w0);
+  return precision == MIXED ? launch_es_variant<2, MIXED, true>(P, w, nullptr, route, n, mag, status, grid, stream)
+                            : launch_es_variant<2, FP64, true>(P, w, nullptr, route, n, mag, status, grid, stream);
+}
+
+size_t es_smem_bytes(const EsParams &P, int nl, bool grad) {
   const int deg = nl * nl + 1;
   size_t b = 0;
   b += sizeof(cd) * (size_t)P.Lcap * deg;
   b += sizeof(double) * P.Lcap * 2;
-  b += sizeof(uint64_t) * P.Lcap * 3;
+  b += sizeof(uint64_t) * P.Lcap * (3 + deg);
   b += (sizeof(MergeState) + 15) / 16 * 16;
   b += sizeof(uint32_t) * (size_t)P.CPcap;
   b += sizeof(int) * (P.Lcap + 1);
   b += sizeof(uint16_t) * P.Lcap * 5;
+  b = (b + 15) / 16 * 16;
+  if (grad) b += 2 * sizeof(cd) * (size_t)P.CPcap;  // P/Q values and dT/dz per contour point
   return (b + 15) / 16 * 16;
 }
 

@@ -126,6 +126,109 @@ __device__ __forceinline__ void wk(const Lens &L, cd z, cd (&W)[5]) {
   W[4] = W[4] * -120.0;
 }
 
+// Forward-mode tangent of terms(): given dW (the tangents of W2..W6) and drho,
+// returns the tangents of (mu0, dquad, dhex), differentiating the same series
+// construction (product rule through the powers of delta, the a_kl solve and the
+// area integrals).  One tangent direction per call.
+static __device__ __noinline__ void terms_tangent(const cd (&W)[5], const cd (&dW)[5], double rho, double drho,
+                                                  double gamma_ld, double &dmu0, double &ddq, double &ddh) {
+  cd c[NC], dc[NC];
+  cd pw[ORD - 1][NC], dpw[ORD - 1][NC];
+  for (int i = 0; i < NC; ++i) {
+    c[i] = dc[i] = mk(0, 0);
+    for (int m = 0; m < ORD - 1; ++m) pw[m][i] = dpw[m][i] = mk(0, 0);
+  }
+  const cd W2c = conj(W[0]), dW2c = conj(dW[0]);
+  const double m0 = 1.0 / (1.0 - norm2(W[0]));
+  const double dm0 = m0 * m0 * 2.0 * (W[0].x * dW[0].x + W[0].y * dW[0].y);
+  c[idx(1, 0)] = (mk(1, 0) + W2c) * m0;
+  dc[idx(1, 0)] = dW2c * m0 + (mk(1, 0) + W2c) * dm0;
+  c[idx(0, 1)] = mk(0, 1) * (mk(1, 0) - W2c) * m0;
+  dc[idx(0, 1)] = mk(0, 1) * ((mk(0, 0) - dW2c) * m0 + (mk(1, 0) - W2c) * dm0);
+  for (int p = 2; p <= ORD; ++p) {
+    for (int m = 2; m <= p; ++m) {
+      for (int l = 0; l <= p; ++l) {
+        cd acc = mk(0, 0), dacc = mk(0, 0);
+        for (int p1 = m - 1; p1 <= p - 1; ++p1) {
+          const int p2 = p - p1;
+          const int lo = max(0, l - p2), hi = min(p1, l);
+          for (int l1 = lo; l1 <= hi; ++l1) {
+            const int l2 = l - l1;
+            const cd lhs = (m == 2) ? c[idx(p1 - l1, l1)] : pw[m - 3][idx(p1 - l1, l1)];
+            const cd dlhs = (m == 2) ? dc[idx(p1 - l1, l1)] : dpw[m - 3][idx(p1 - l1, l1)];
+            const cd r = c[idx(p2 - l2, l2)], dr = dc[idx(p2 - l2, l2)];
+            acc = cfma(lhs, r, acc);
+            dacc = cfma(dlhs, r, cfma(lhs, dr, dacc));
+          }
+        }
+        pw[m - 2][idx(p - l, l)] = acc;
+        dpw[m - 2][idx(p - l, l)] = dacc;
+      }
+    }
+    for (int l = 0; l <= p; ++l) {
+      const int k = p - l;
+      cd Q = mk(0, 0), dQ = mk(0, 0);
+      for (int m = 2; m <= p; ++m) {
+        const double f = 1.0 / kfact(m);
+        Q = Q + W[m - 1] * pw[m - 2][idx(k, l)] * f;
+        dQ = dQ + (dW[m - 1] * pw[m - 2][idx(k, l)] + W[m - 1] * dpw[m - 2][idx(k, l)]) * f;
+      }
+      const double kl = kfact(k) * kfact(l);
+      Q = Q * kl;
+      dQ = dQ * kl;
+      const cd base = conj(Q) + W2c * Q;
+      const cd dbase = conj(dQ) + dW2c * Q + W2c * dQ;
+      c[idx(k, l)] = base * (m0 / kl);
+      dc[idx(k, l)] = (dbase * m0 + base * dm0) * (1.0 / kl);
+    }
+  }
+  double A[3], dA[3];
+  for (int mi = 0; mi < 3; ++mi) {
+    const int m = 2 + 2 * mi;
+    double acc = 0.0, dacc = 0.0;
+    for (int p = max(1, m - ORD); p <= min(ORD, m - 1); ++p) {
+      const int q = m - p;
+      for (int lp = 0; lp <= p; ++lp)
+        for (int lq = 0; lq <= q; ++lq) {
+          const int kp = p - lp, kq = q - lq;
+          double t = 0.0;
+          if (kq > 0) t -= kq * trig_moment(kp + kq - 1, lp + lq + 1);
+          if (lq > 0) t += lq * trig_moment(kp + kq + 1, lp + lq - 1);
+          if (t != 0.0) {
+            const cd a = c[idx(kp, lp)], b = c[idx(kq, lq)], da = dc[idx(kp, lp)], db = dc[idx(kq, lq)];
+            acc += (a.x * b.y - a.y * b.x) * t;
+            dacc += ((da.x * b.y - da.y * b.x) + (a.x * db.y - a.y * db.x)) * t;
+          }
+        }
+    }
+    A[mi] = 0.5 * acc / 3.14159265358979323846;
+    dA[mi] = 0.5 * dacc / 3.14159265358979323846;
+  }
+  dmu0 = dA[0];
+  const double fq = (1.0 - gamma_ld / 5.0), fh = (1.0 - 11.0 * gamma_ld / 35.0);
+  ddq = fq * (dA[1] * rho * rho + A[1] * 2.0 * rho * drho);
+  ddh = fh * (dA[2] * rho * rho * rho * rho + A[2] * 4.0 * rho * rho * rho * drho);
+}
+
+// Tangent of W_k (k = 2..6) of a binary lens along (dz, da, de1):
+// W_k = c_k [e1 (z - a)^-k + (1 - e1) (z + a)^-k], c_k = (-1)^(k-1) (k-1)!.
+__device__ __forceinline__ void wk_tangent_binary(const Lens &L, cd z, cd dz, double da, double de1, cd (&dW)[5]) {
+  const double a = L.r[0].x, e1 = L.eps[0], e2 = L.eps[1];
+  const cd u = crecip(z - mk(a, 0)), v = crecip(z + mk(a, 0));
+  cd pu = u, pv = v;  // u^(k-1), v^(k-1) at k = 2
+  const double ck[5] = {-1.0, 2.0, -6.0, 24.0, -120.0};
+  for (int k = 0; k < 5; ++k) {
+    const int m = k + 2;
+    const cd um = pu * u, vm = pv * v;          // u^m, v^m
+    const cd um1 = um * u, vm1 = vm * v;        // u^(m+1), v^(m+1)
+    // d[(z - a)^-m] = -m (z - a)^-(m+1) (dz - da); d[(z + a)^-m] = -m (z + a)^-(m+1) (dz + da)
+    const cd t = (um - vm) * de1 + um1 * (dz - mk(da, 0)) * (-(double)m * e1) + vm1 * (dz + mk(da, 0)) * (-(double)m * e2);
+    dW[k] = t * ck[k];
+    pu = um;
+    pv = vm;
+  }
+}
+
 }  // namespace hexa
 
 // Binary-lens proximity test (lightcurve.py:23-75) with c_m=1e-2, gamma=0.02,

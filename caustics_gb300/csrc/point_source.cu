@@ -8,6 +8,7 @@
 // 16-byte words (coefficients in, roots out).
 #include "aberth.cuh"
 #include "hexadecapole.cuh"
+#include "es.h"
 #include "internal.h"
 
 namespace cgb {
@@ -199,6 +200,125 @@ cudaError_t launch_lc_points(const Lens &L, double q, const double *w, double rh
     lc_points_kernel<3><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, precision, status);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---- batched light curves ----
+// Point i belongs to curve c with offsets[c] <= i < offsets[c+1]; its source is
+// on the curve's rectilinear trajectory at times[i] (trajectory.py:152-155 with
+// pi_E = 0): w = (u0 cos a + tau sin a) + i (-u0 sin a + tau cos a), tau = (t - t0)/tE.
+__device__ __forceinline__ int64_t curve_of(const int64_t *offsets, int64_t ncurves, int64_t i) {
+  int64_t lo = 0, hi = ncurves - 1;
+  while (lo < hi) {
+    int64_t mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Per-point pass of batched mag(): images, hexadecapole, routing tests; points
+// that need the contour integral are appended to the device work queue
+// (qcount, qlist).  With GRAD, hexadecapole-routed points also add their
+// cotangent-weighted gradient to cgrad[curve][(s, q, rho, u1, u0, alpha, t0, tE)]
+// (forward-mode tangents through the images and the multipole series).
+template <bool GRAD>
+__global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
+    const CurveDev *__restrict__ curves, const int64_t *__restrict__ offsets, const double *__restrict__ times,
+    int64_t ncurves, int64_t n, double *__restrict__ mag, uint8_t *__restrict__ route, uint32_t *__restrict__ status,
+    int itmax, int precision, unsigned long long *qcount, int64_t *qlist, const double *__restrict__ cot,
+    double *cgrad) {
+  const int64_t i = (int64_t)blockIdx.x * PS_THREADS + threadIdx.x;
+  if (i >= n) return;
+  const int64_t c = curve_of(offsets, ncurves, i);
+  const CurveDev cv = curves[c];
+  const Lens L = make_lens(2, cv.s, cv.q, 0.0, 0.0, 0.0);
+  const double tau = (times[i] - cv.t0) / cv.tE;
+  double sa, ca;
+  sincos(cv.alpha, &sa, &ca);
+  const cd wi = mk(cv.u0 * ca + tau * sa + L.x_cm, -cv.u0 * sa + tau * ca);
+  uint32_t flags = 0;
+  cd z[5];
+  uint32_t m = images<2>(L, wi, z, itmax, precision, flags);
+  double mu_multi = 0.0, dmu = 0.0;
+  cd W[5][5];
+  double val[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    val[k] = 0.0;
+    if (!((m >> k) & 1u)) continue;
+    hexa::wk<2>(L, z[k], W[k]);
+    double mu0, dq, dh;
+    hexa::terms(W[k], cv.rho, 0.0, mu0, dq, dh);
+    val[k] = mu0 + dq + dh;
+    mu_multi += fabs(val[k]);
+    dmu += fabs(dq) + fabs(dh);
+  }
+  bool hex_ok = proximity_test_binary(L, wi, z, m, cv.rho, dmu);
+  if (cv.q < 0.01) hex_ok = hex_ok && planetary_test(L, wi, cv.rho);
+  mag[i] = mu_multi;
+  route[i] = hex_ok ? 0 : 1;
+  if (status) status[i] = flags;
+  if (!hex_ok) {
+    const unsigned long long slot = atomicAdd(qcount, 1ull);
+    qlist[slot] = i;
+    return;
+  }
+  if (!GRAD) return;
+  // tangents along (a, e1, rho, Re w0, Im w0)
+  const double a = L.r[0].x, e1 = L.eps[0], e2 = L.eps[1];
+  double d[5];
+  for (int dir = 0; dir < 5; ++dir) {
+    const double da = dir == 0, de1 = dir == 1, drho = dir == 2;
+    const cd dw0 = mk(dir == 3, dir == 4);
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      if (!((m >> k) & 1u)) continue;
+      const cd zb = conj(z[k]);
+      const cd u = crecip(zb - mk(a, 0)), v = crecip(zb + mk(a, 0));
+      const cd lam = u * u * e1 + v * v * e2;
+      const cd fa = u * u * e1 - v * v * e2, fe = u - v;
+      const cd g = dw0 + fa * da + fe * de1;
+      const cd dz = cdiv(g - lam * conj(g), mk(1.0 - norm2(lam), 0.0));
+      cd dW[5];
+      hexa::wk_tangent_binary(L, z[k], dz, da, de1, dW);
+      double dmu0, ddq, ddh;
+      hexa::terms_tangent(W[k], dW, cv.rho, drho, 0.0, dmu0, ddq, ddh);
+      acc += (val[k] > 0 ? 1.0 : (val[k] < 0 ? -1.0 : 0.0)) * (dmu0 + ddq + ddh);
+    }
+    d[dir] = acc;
+  }
+  const double q = cv.q, opq = 1.0 + q, ah = 0.5 * cv.s;
+  const double ds = 0.5 * d[0] + d[3] * (1.0 - q) / (2.0 * opq);
+  const double dqq = -d[1] / (opq * opq) - d[3] * 2.0 * ah / (opq * opq);
+  const double du0 = d[3] * ca - d[4] * sa;
+  const double dal = d[3] * (-cv.u0 * sa + tau * ca) + d[4] * (-cv.u0 * ca - tau * sa);
+  const double dt0 = -(d[3] * sa + d[4] * ca) / cv.tE;
+  const double dtE = -tau * (d[3] * sa + d[4] * ca) / cv.tE;
+  const double ct = cot ? cot[i] : 1.0;
+  double *gp = cgrad + c * 8;
+  atomicAdd(gp + 0, ct * ds);
+  atomicAdd(gp + 1, ct * dqq);
+  atomicAdd(gp + 2, ct * d[2]);
+  atomicAdd(gp + 4, ct * du0);
+  atomicAdd(gp + 5, ct * dal);
+  atomicAdd(gp + 6, ct * dt0);
+  atomicAdd(gp + 7, ct * dtE);
+}
+
+cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
+                                     int precision, unsigned long long *qcount, int64_t *qlist, bool grad,
+                                     cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+  if (grad)
+    lc_points_batched_kernel<true><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n, mag,
+                                                                    route, status, P.itmax, precision, qcount, qlist,
+                                                                    P.cot, P.cgrad);
+  else
+    lc_points_batched_kernel<false><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n, mag,
+                                                                     route, status, P.itmax, precision, qcount, qlist,
+                                                                     nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define CGB_ABI_VERSION 1
+#define CGB_ABI_VERSION 2
 
 /* launch status */
 #define CGB_OK 0
@@ -59,7 +59,17 @@ typedef struct cgb_es_options {
   int32_t roots_itmax;    /* reference default 2500 */
   int32_t precision;      /* CGB_PREC_FP64 or CGB_PREC_MIXED */
   int32_t grid;           /* CTAs to launch, 0 = automatic */
+  int32_t queue_chunk;    /* batched light curves: work items taken per queue grab (>= 1) */
 } cgb_es_options;
+
+/* Parameters of one binary-lens light curve for the batched entry points: lens
+ * (s, q), source radius and linear limb darkening (rho, u1), and the
+ * rectilinear trajectory w(t) = (u0 cos alpha + tau sin alpha)
+ * + i (-u0 sin alpha + tau cos alpha), tau = (t - t0) / tE
+ * (src/caustics/trajectory.py:152-155 with pi_E = 0). */
+typedef struct cgb_curve_params {
+  double s, q, rho, u1, u0, alpha, t0, tE;
+} cgb_curve_params;
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *cgb_last_error(void);
@@ -101,11 +111,47 @@ int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t 
 int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                             const cgb_es_options *opts, uint32_t *status, void *stream);
 
+/* Adjoint of cgb_mag_extended_source for binary lenses: mag float64[n] and
+ * grad float64[n, 6] = d mag / d(s, q, rho, u1, Re w0, Im w0) of the discretised
+ * contour integral (the limb sampling, segment linking and merging decisions
+ * are piecewise constant, as under the reference's autodiff).  The contours are
+ * recomputed in the backward pass, not stored.  The reference differentiates
+ * mag_extended_source with JAX autodiff through the root primitive's JVP
+ * (src/caustics/ehrlich_aberth_primitive.py:254-324). */
+int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                 cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status, void *stream);
+
 /* Light curve: hexadecapole where the reference's proximity tests accept it,
  * contour integration elsewhere.  route: uint8[n] output, 1 where the contour
  * integral was used.  Replaces mag (src/caustics/lightcurve.py:99-254). */
 int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
             const cgb_es_options *opts, uint32_t *status, void *stream);
+
+/* Workspace (device bytes) the batched entry points need for npoints points:
+ * a work-queue header and one queue slot per point. */
+size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints);
+
+/* mag() of ncurves binary-lens light curves of uneven lengths in one pass:
+ * points offsets[c] .. offsets[c+1]-1 (int64, device) belong to curve c
+ * (curves: cgb_curve_params[ncurves], device) at times t (float64[npoints]).
+ * The per-point pass computes the hexadecapole and the routing tests and queues
+ * the points that need contour integration; a persistent kernel then drains
+ * the device queue.  mag float64[npoints], route uint8[npoints] (1 = contour).
+ * Replaces a loop of mag() calls (src/caustics/lightcurve.py:99-254), one per
+ * curve. */
+int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
+                       int64_t npoints, double *mag, uint8_t *route, uint32_t *status, const cgb_es_options *opts,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* Vector-Jacobian product of cgb_mag_lc_batched: grad float64[ncurves, 8] =
+ * sum over the curve's points of cot[i] * d mag_i / d(s, q, rho, u1, u0,
+ * alpha, t0, tE).  Hand-written adjoint: implicit-function rule for the images,
+ * forward-mode tangents through the hexadecapole, reverse mode through the
+ * contour integral with the contours recomputed.  Also writes mag and route. */
+int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
+                           int64_t npoints, const double *cot, double *grad, double *mag, uint8_t *route,
+                           uint32_t *status, const cgb_es_options *opts, void *workspace, size_t workspace_bytes,
+                           void *stream);
 
 /* Diagnostics (no counterpart in the reference): cgb_mag_extended_source that
  * also writes, per point, a record of cgb_debug_record_len(npts_limb) doubles:

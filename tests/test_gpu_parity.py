@@ -170,7 +170,8 @@ def test_hexadecapole_routing(G, tag):
                      return_route=True)
     assert np.array_equal(route, ~test)
     ok = test
-    assert np.max(np.abs(m[ok] - d["mu_multi"][ok]) / d["mu_multi"][ok]) < 1e-10
+    if ok.any():  # for q < 0.01 the reference's planetary test accepts no point (lightcurve.py:81)
+        assert np.max(np.abs(m[ok] - d["mu_multi"][ok]) / d["mu_multi"][ok]) < 1e-10
 
 
 @pytest.mark.parametrize("ld", [False, True])
