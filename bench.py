@@ -164,6 +164,130 @@ def run_reference(args):
 # our arm
 # ---------------------------------------------------------------------------
 
+def draw_batched(ncurves_total, seed, nmin, nmax, take):
+    """Curves drawn as the reference-scale batched workloads: per curve
+    s ~ logU[0.3, 3], q ~ logU[1e-4, 1], rho ~ logU[1e-3, 1e-1], u0 ~ U[-0.3, 0.3],
+    alpha ~ U[0, 2pi], u1 ~ U[0.2, 0.8], tE ~ logU[5, 100], t0 = 0, length
+    ~ U{nmin..nmax}, times uniform on [t0 - 2tE, t0 + 2tE]; the first `take`
+    curves of the full draw."""
+    rng = np.random.default_rng(seed)
+    n = ncurves_total
+    lens = rng.integers(nmin, nmax + 1, n)
+    cv = np.stack([10 ** rng.uniform(np.log10(0.3), np.log10(3), n), 10 ** rng.uniform(-4, 0, n),
+                   10 ** rng.uniform(-3, -1, n), rng.uniform(0.2, 0.8, n), rng.uniform(-0.3, 0.3, n),
+                   rng.uniform(0, 2 * np.pi, n), np.zeros(n), 10 ** rng.uniform(np.log10(5), 2, n)], axis=1)
+    ts = [np.sort(rng.uniform(-2 * te, 2 * te, m)) for te, m in zip(cv[:take, 7], lens[:take])]
+    offsets = np.concatenate([[0], np.cumsum(lens[:take])]).astype(np.int64)
+    return offsets, np.concatenate(ts), cv[:take]
+
+
+def timed(stream, fn, reps=1, flush=None):
+    import torch
+    ms = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms))
+
+
+def extras_batched(C, dev, stream, flush, ncurves=24, plain_points=24):
+    """A bounded sample of the 4096-curve uneven batched workload (seed 2,
+    lengths U{200..5000}, npts_limb=200, npts_ld=100, LD): batched mixed with
+    the autotuned launch shape in a CUDA graph, against the plain per-call FP64
+    form (one launch per full-contour point) on points of the same curves."""
+    import torch
+    off, t, cv = draw_batched(4096, 2, 200, 5000, ncurves)
+    kw = dict(npts_limb=200, limb_darkening=True, npts_ld=100)
+    ev = C.BatchedLightCurves(off, t, curves_for_tuning=cv, precision="mixed", **kw)
+    cvd = torch.as_tensor(cv, device=dev)
+    ev(cvd)
+    ms = timed(stream, lambda: ev(cvd), reps=3, flush=flush)
+    route = ev.route.bool().cpu().numpy()
+    nfull = int(route.sum())
+    ref = C.mag_lc_batched(off, t, cv, precision="fp64", **kw).cpu().numpy()
+    err = float(np.max(np.abs(ev.mag.cpu().numpy() - ref) / ref))
+    # plain per-call FP64 on a sample of the full-contour points
+    full = np.flatnonzero(route)
+    pick = full[np.linspace(0, len(full) - 1, min(plain_points, len(full))).astype(int)]
+    curve_of = np.searchsorted(off, pick, side="right") - 1
+    calls = []
+    for i, c in zip(pick, curve_of):
+        s_, q_, rho, u1, u0, a, t0, te = cv[c]
+        tau = (t[i] - t0) / te
+        w = torch.tensor([(u0 * np.cos(a) + tau * np.sin(a)) + 1j * (-u0 * np.sin(a) + tau * np.cos(a))],
+                         dtype=torch.complex128, device=dev)
+        calls.append((w, rho, dict(npts_limb=200, limb_darkening=True, u1=u1, npts_ld=100, s=s_, q=q_)))
+
+    def plain():
+        for w, rho, k in calls:
+            C.mag_extended_source(w, rho, precision="fp64", grid=1, **k)
+    plain()
+    pms = timed(stream, plain)
+    plain_rate = len(calls) / (pms * 1e-3)
+    return {"workload": f"first {ncurves} of 4096 curves, seed 2, lengths U{{200..5000}}, npts_limb 200, npts_ld 100, LD",
+            "points": int(len(t)), "full_contour_points": nfull, "ms": ms, "points_per_s": len(t) / (ms * 1e-3),
+            "full_contour_evals_per_s": nfull / (ms * 1e-3), "plain_fp64_per_call_evals_per_s": plain_rate,
+            "batched_full_vs_plain_fp64": nfull / (ms * 1e-3) / plain_rate, "mixed_vs_fp64_max_rel_err": err,
+            "autotuned": ev.config, "cuda_graph": ev.graph is not None}
+
+
+def extras_vjp(C, dev, stream, flush):
+    """VJP with respect to (s, q, rho, u1, u0, alpha, t0, tE) for 256 curves x
+    1000 points drawn as the batched workload (seed 3), N(0,1) cotangent."""
+    import torch
+    off, t, cv = draw_batched(256, 3, 1000, 1000, 256)
+    kw = dict(npts_limb=200, limb_darkening=True, npts_ld=100)
+    offd, td, cvd = (torch.as_tensor(x, device=dev) for x in (off, t, cv))
+    cot = torch.as_tensor(np.random.default_rng(3).normal(size=len(t)), device=dev)
+    C.mag_lc_batched_vjp(offd, td, cvd, cot, precision="mixed", **kw)
+    vms = timed(stream, lambda: C.mag_lc_batched_vjp(offd, td, cvd, cot, precision="mixed", **kw), reps=2, flush=flush)
+    fms = timed(stream, lambda: C.mag_lc_batched(offd, td, cvd, precision="mixed", **kw), reps=2, flush=flush)
+    g32, _ = C.mag_lc_batched_vjp(offd, td, cvd, cot, precision="mixed", **kw)
+    g64, _ = C.mag_lc_batched_vjp(offd, td, cvd, cot, precision="fp64", **kw)
+    rel = (torch.abs(g32 - g64) / torch.clamp(torch.abs(g64), min=1e-300)).median().item()
+    return {"workload": "256 curves x 1000 points, seed 3, npts_limb 200, npts_ld 100, LD, cotangent N(0,1)",
+            "vjp_points_per_s": len(t) / (vms * 1e-3), "forward_points_per_s": len(t) / (fms * 1e-3),
+            "vjp_over_forward_time": vms / fms, "mixed_vs_fp64_grad_median_rel_diff": rel}
+
+
+def extras_triple(C, dev, stream, nsys=1000, per_sys=1000, big=1 << 20):
+    """Triple-lens point source, mixed (FP32 Aberth + compensated double-float
+    Horner + FP64 polish) against FP64: 1000 systems x 1000 positions (seed 1,
+    s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4, 1e-1], psi ~ U[0, 2pi];
+    s = s1, q = q1, q3 = q2, r3 = s2).  Throughput from one 2^20-position call."""
+    import torch
+    rng = np.random.default_rng(1)
+    sysp = np.stack([rng.uniform(0.5, 2, nsys), rng.uniform(0.5, 2, nsys), 10 ** rng.uniform(-4, 0, nsys),
+                     10 ** rng.uniform(-4, -1, nsys), rng.uniform(0, 2 * np.pi, nsys)], axis=1)
+    w = rng.uniform(-1.5, 1.5, (nsys, per_sys)) + 1j * rng.uniform(-1.5, 1.5, (nsys, per_sys))
+    wd = torch.as_tensor(w, device=dev)
+    maxerr, count_mismatch, root_err = 0.0, 0, 0.0
+    for k in range(nsys):
+        p = dict(s=sysp[k, 0], q=sysp[k, 2], q3=sysp[k, 3], r3=sysp[k, 1], psi=sysp[k, 4])
+        m64, z64, k64 = C.mag_point_source(wd[k], nlenses=3, precision="fp64", return_images=True, **p)
+        m32, z32, k32 = C.mag_point_source(wd[k], nlenses=3, precision="mixed", return_images=True, **p)
+        maxerr = max(maxerr, float((torch.abs(m32 - m64) / m64).max().item()))
+        count_mismatch += int((k32 != k64).sum().item())
+        d = torch.abs(z32[:, :, None] - z64[:, None, :]).min(dim=2).values / torch.clamp(torch.abs(z64), min=1e-300)
+        root_err = max(root_err, float(d.max().item()))
+    p = dict(s=sysp[0, 0], q=sysp[0, 2], q3=sysp[0, 3], r3=sysp[0, 1], psi=sysp[0, 4])
+    wb = torch.as_tensor(rng.uniform(-1.5, 1.5, big) + 1j * rng.uniform(-1.5, 1.5, big), device=dev)
+    rate = {}
+    for prec in ("fp64", "mixed"):
+        C.mag_point_source(wb, nlenses=3, precision=prec, **p)
+        rate[prec] = big / (timed(stream, lambda: C.mag_point_source(wb, nlenses=3, precision=prec, **p), 3) * 1e-3)
+    return {"workload": "1000 systems x 1000 positions, seed 1 (throughput: 2^20 positions of system 0)",
+            "fp64_evals_per_s": rate["fp64"], "mixed_evals_per_s": rate["mixed"],
+            "mixed_vs_fp64_max_rel_mag_err": maxerr, "image_count_mismatches": count_mismatch,
+            "max_rel_root_err": root_err}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -171,11 +295,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-points", type=int, default=40)
+    ap.add_argument("--points", type=int, default=WL["npoints"], help="trajectory points (smaller: profiling case)")
+    ap.add_argument("--quick", action="store_true", help="headline step only: no CPU baseline, no extra workloads")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.points != WL["npoints"]:
+        WL["npoints"] = args.points
+        WL["workload"] = f"binary-ld-lightcurve-{args.points}pt"
+    if args.quick:
+        args.no_cpu = True
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -195,22 +326,33 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     w_host = trajectory(WL["npoints"])
+    t_host = np.linspace(WL["t0"] - 2 * WL["tE"], WL["t0"] + 2 * WL["tE"], WL["npoints"])
+    curves_host = np.array([[WL["s"], WL["q"], WL["rho"], WL["u1"], WL["u0"], WL["alpha"], WL["t0"], WL["tE"]]])
+    offsets_host = np.array([0, WL["npoints"]], dtype=np.int64)
     w = torch.as_tensor(w_host).to(dev)
+    t_dev = torch.as_tensor(t_host).to(dev)
+    curves = torch.as_tensor(curves_host).to(dev)
+    offsets = torch.as_tensor(offsets_host).to(dev)
+    cot = torch.randn(WL["npoints"], dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(3))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     kw = dict(npts_limb=WL["npts_limb"], limb_darkening=True, u1=WL["u1"], npts_ld=WL["npts_ld"], s=WL["s"],
               q=WL["q"])
+    kwb = dict(npts_limb=WL["npts_limb"], limb_darkening=True, npts_ld=WL["npts_ld"])
 
-    def step(prec):
-        return C.mag(w, WL["rho"], precision=prec, **kw)
+    # batched path: per-point pass + persistent contour kernel draining the
+    # device queue, launch shape from the autotuner, captured in a CUDA graph
+    ev = C.BatchedLightCurves(offsets, t_dev, curves_for_tuning=curves, precision="mixed", **kwb)
+
+    def step():
+        return ev(curves)
 
     def barrier():
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
 
-    # warm-up
     for _ in range(args.warmup):
-        out_mixed = step("mixed")
+        step()
     barrier()
     # timed batched mixed steps (events on the launching stream, L2 flushed between)
     clocks = Clocks(local)
@@ -221,12 +363,13 @@ def main():
         flush.fill_(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        out_mixed = step("mixed")
+        step()
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
     barrier()
     clk = clocks.stop()
+    out_mixed = ev.mag.clone()
     ms = float(np.mean(times))
     if dist is not None:
         t = torch.tensor([ms], device=dev)
@@ -235,90 +378,108 @@ def main():
     value = world * WL["npoints"] / (ms * 1e-3)
 
     # dominant kernel alone: the contour pass over all points (every point routes to it)
-    es_ms = []
-    for _ in range(max(2, args.steps // 2)):
-        flush.fill_(1)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        C.mag_extended_source(w, WL["rho"], precision="mixed", **kw)
-        e1.record(stream)
-        e1.synchronize()
-        es_ms.append(e0.elapsed_time(e1))
-    es_ms = float(np.mean(es_ms))
-
-    # FP64 batched, and plain per-call FP64 (one launch per point, like lax.map)
-    step("fp64")
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    out64 = step("fp64")
-    e1.record(stream)
-    e1.synchronize()
-    fp64_rate = WL["npoints"] / (e0.elapsed_time(e1) * 1e-3)
-    err = float(torch.max(torch.abs(out_mixed - out64) / out64).item())
-    idx = np.linspace(0, WL["npoints"] - 1, args.plain_points).astype(int)
-    wp = [w[i:i + 1] for i in idx]
-    C.mag_extended_source(wp[0], WL["rho"], precision="fp64", grid=1, **kw)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for x in wp:
-        C.mag_extended_source(x, WL["rho"], precision="fp64", grid=1, **kw)
-    e1.record(stream)
-    e1.synchronize()
-    plain_rate = len(wp) / (e0.elapsed_time(e1) * 1e-3)
-
-    # end to end through the public API with host buffers
-    C.mag(w_host, WL["rho"], precision="mixed", **kw)
-    e2e_t = []
-    for _ in range(max(2, args.steps)):
-        t = time.perf_counter()
-        res = C.mag(w_host, WL["rho"], precision="mixed", **kw)
-        e2e_t.append(time.perf_counter() - t)
-    e2e_rate = world * WL["npoints"] / float(np.mean(e2e_t))
-
-    # live FMA-pipe peak (FP32) for the roofline denominator
+    es_ms = timed(stream, lambda: C.mag_extended_source(w, WL["rho"], precision="mixed", **kw),
+                  reps=max(2, args.steps // 2), flush=flush)
+    achieved = WL["npoints"] * FLOP_PER_EVAL / (es_ms * 1e-3) / 1e12
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     buf = torch.empty(sms * 8, dtype=torch.float64, device=dev)
-    iters, blocks = 4096, sms * 8
     import ctypes
-    L.lib().cgb_probe_fma(0, iters, blocks, ctypes.c_void_p(buf.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
-    e0.record(stream)
-    L.lib().cgb_probe_fma(0, iters, blocks, ctypes.c_void_p(buf.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
-    e1.record(stream)
-    e1.synchronize()
-    fp32_peak = blocks * 256 * iters * 256 / (e0.elapsed_time(e1) * 1e-3) / 1e12
-    achieved = WL["npoints"] * FLOP_PER_EVAL / (es_ms * 1e-3) / 1e12
 
-    cpu = None
-    if pool is not None:
-        rate, n = cpu_rate(pool, cores)
-        pool.close()
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} trajectory points, oracle restatement (NumPy + C solver), spawn pool"}
+    def fma_peak(fp64):
+        iters, blocks = (4096, sms * 8) if not fp64 else (512, sms * 8)
+        launch = lambda: L.lib().cgb_probe_fma(fp64, iters, blocks, ctypes.c_void_p(buf.data_ptr()),
+                                               ctypes.c_void_p(stream.cuda_stream))
+        launch()
+        return blocks * 256 * iters * 256 / (timed(stream, launch) * 1e-3) / 1e12
+    fp32_peak = fma_peak(0)
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
+        "config": {**WL, "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas",
+                   "autotuned": ev.config, "cuda_graph": ev.graph is not None},
+        "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None, "kernel": "es_kernel<2,MIXED>",
+                     "peak_source": "measured live in bench.py (cgb_probe_fma, FP32 FMA burst); the path moves "
+                                    "24 B per evaluation, so neither HBM nor tensor peaks bound it",
+                     "flop_per_eval": FLOP_PER_EVAL,
+                     "hbm_sanity": {"bytes_per_eval": 24,
+                                    "achieved_gbs": 24 * WL["npoints"] / (es_ms * 1e-3) / 1e9,
+                                    "peak_gbs_measured": _measured_peaks().get("hbm_gbs")}},
+        "clocks": clk,
+        "gpu_launches": 2 * args.steps,  # per step: the per-point pass and the persistent contour kernel
+    }
+    if not args.quick:
+        # FP64 batched, and plain per-call FP64 (one launch per point, like lax.map)
+        C.mag_lc_batched(offsets, t_dev, curves, precision="fp64", **kwb)
+        out64 = None
 
-    if rank == 0:
-        print(json.dumps({
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
-            "config": {**WL, "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"},
-            "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp32_peak, "traffic": None, "kernel": "es_kernel<2,MIXED>",
-                         "peak_source": "measured live in bench.py (cgb_probe_fma, FP32 FMA burst)",
-                         "flop_per_eval": FLOP_PER_EVAL},
-            "cpu_baseline": cpu,
-            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": WL["npoints"] * 16,
+        def f64():
+            nonlocal out64
+            out64 = C.mag_lc_batched(offsets, t_dev, curves, precision="fp64", **kwb)
+        fp64_ms = timed(stream, f64, flush=flush)
+        fp64_rate = WL["npoints"] / (fp64_ms * 1e-3)
+        err = float(torch.max(torch.abs(out_mixed - out64) / out64).item())
+        idx = np.linspace(0, WL["npoints"] - 1, args.plain_points).astype(int)
+        wp = [w[i:i + 1] for i in idx]
+        C.mag_extended_source(wp[0], WL["rho"], precision="fp64", grid=1, **kw)
+
+        def plain():
+            for x in wp:
+                C.mag_extended_source(x, WL["rho"], precision="fp64", grid=1, **kw)
+        plain_rate = len(wp) / (timed(stream, plain) * 1e-3)
+        fp64_peak = fma_peak(1)
+        es64_ms = timed(stream, lambda: C.mag_extended_source(w, WL["rho"], precision="fp64", **kw), flush=flush)
+
+        # VJP of the light curve (s, q, rho, u1, u0, alpha, t0, tE) with a N(0,1) cotangent
+        C.mag_lc_batched_vjp(offsets, t_dev, curves, cot, precision="mixed", **ev.config, **kwb)
+        vjp_ms = timed(stream, lambda: C.mag_lc_batched_vjp(offsets, t_dev, curves, cot, precision="mixed",
+                                                            **ev.config, **kwb), reps=max(2, args.steps // 2),
+                       flush=flush)
+        vjp_rate = WL["npoints"] / (vjp_ms * 1e-3)
+
+        # end to end through the public API with host buffers (H2D of times and curve
+        # parameters, D2H of the magnifications inside the timed region)
+        C.mag_lc_batched(offsets_host, t_host, curves_host, precision="mixed", **ev.config, **kwb).cpu()
+        e2e_t = []
+        for _ in range(max(2, args.steps)):
+            t = time.perf_counter()
+            C.mag_lc_batched(offsets_host, t_host, curves_host, precision="mixed", **ev.config, **kwb).cpu().numpy()
+            e2e_t.append(time.perf_counter() - t)
+        e2e_rate = world * WL["npoints"] / float(np.mean(e2e_t))
+        res.update({
+            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": WL["npoints"] * 8 + 16 + 64,
                     "d2h_bytes_per_step": WL["npoints"] * 8},
-            "clocks": clk,
-            "gpu_launches": 2 * args.steps,
             "plain_fp64_per_call_evals_per_s": plain_rate,
             "batched_fp64_evals_per_s": fp64_rate,
             "batched_mixed_vs_plain_fp64": value / world / plain_rate,
             "mixed_vs_fp64_max_rel_err": err,
-            "vjp_evals_per_s": None,
-        }))
+            "vjp_evals_per_s": vjp_rate,
+            "vjp_plus_forward_vs_plain_fp64": 1.0 / ((1.0 / value * world + 1.0 / vjp_rate) * plain_rate),
+            "fp64_roofline": {"kernel": "es_kernel<2,FP64>", "achieved": WL["npoints"] * FLOP_PER_EVAL /
+                              (es64_ms * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                              "peak_source": "measured live (cgb_probe_fma, FP64 FMA)"},
+            "batched_4096_curve_sample": extras_batched(C, dev, stream, flush),
+            "vjp_256x1000": extras_vjp(C, dev, stream, flush),
+            "triple_point_source": extras_triple(C, dev, stream),
+        })
+    if pool is not None:
+        rate, n = cpu_rate(pool, cores)
+        pool.close()
+        res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"{n} trajectory points, oracle restatement (NumPy + C solver), spawn pool"}
+    if rank == 0:
+        print(json.dumps(res))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 if __name__ == "__main__":

@@ -4,6 +4,7 @@ extended-source (contour-integration) magnification, hexadecapole routing —
 behind a C ABI (include/caustics_gb300.h) with the reference's Python
 signatures."""
 from .api import (  # noqa: F401
+    BatchedLightCurves,
     LightCurveMagnification,
     ehrlich_aberth,
     mag_extended_source_grad,
@@ -18,4 +19,4 @@ from .api import (  # noqa: F401
 )
 
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
-           "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification"]
+           "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves"]

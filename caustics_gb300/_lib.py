@@ -35,7 +35,7 @@ class LensParams(ctypes.Structure):
 class EsOptions(ctypes.Structure):
     _fields_ = [("npts_limb", ctypes.c_int32), ("limb_darkening", ctypes.c_int32), ("u1", ctypes.c_double),
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32)]
+                ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32)]
 
 
 class CurveParams(ctypes.Structure):

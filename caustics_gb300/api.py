@@ -176,9 +176,9 @@ def mag_point_source(w, nlenses=2, roots_itmax=2500, roots_compensated=False, pr
     return out[0] if len(out) == 1 else tuple(out)
 
 
-def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0):
+def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1):
     return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
-                       _precision(precision or "fp64"), int(grid))
+                       _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group))
 
 
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
@@ -251,7 +251,8 @@ def _workspace(n, device):
 
 
 def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
-                   precision="mixed", grid=0, queue_chunk=1, return_route=False, return_status=False):
+                   precision="mixed", grid=0, queue_chunk=1, ld_group=1, return_route=False, return_status=False,
+                   out=None):
     """mag() for many binary-lens light curves of uneven lengths in one pass.
 
     offsets: int64 [ncurves+1]; t: float64 [npoints]; curves: float64
@@ -260,12 +261,15 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
     off, tt, cv = _batched_args(offsets, t, curves)
     n = tt.numel()
     dev = tt.device
-    mag_out = torch.empty(n, dtype=torch.float64, device=dev)
-    route = torch.empty(n, dtype=torch.uint8, device=dev)
-    st = torch.zeros(n, dtype=torch.int32, device=dev)
-    ws, nbytes = _workspace(n, dev)
-    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid)
-    opts.queue_chunk = int(queue_chunk)
+    if out is None:
+        mag_out = torch.empty(n, dtype=torch.float64, device=dev)
+        route = torch.empty(n, dtype=torch.uint8, device=dev)
+        st = torch.zeros(n, dtype=torch.int32, device=dev)
+        ws, nbytes = _workspace(n, dev)
+    else:  # caller-owned buffers (fixed-shape / graph-captured use)
+        mag_out, route, st, ws = out
+        nbytes = ws.numel()
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
                                            _ptr(st), opts, _ptr(ws), nbytes, _stream()), "cgb_mag_lc_batched")
@@ -278,7 +282,7 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
 
 
 def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
-                       precision="mixed", grid=0, queue_chunk=1):
+                       precision="mixed", grid=0, queue_chunk=1, ld_group=1):
     """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c]."""
     off, tt, cv = _batched_args(offsets, t, curves)
     ct, _ = _to_device(cot, torch.float64)
@@ -288,8 +292,7 @@ def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=Fa
     route = torch.empty(n, dtype=torch.uint8, device=dev)
     grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
     ws, nbytes = _workspace(n, dev)
-    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid)
-    opts.queue_chunk = int(queue_chunk)
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched_vjp(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
                                                _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
@@ -332,3 +335,60 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
                                                      L.lens_params(nlenses, params), opts, None, _stream()),
                 "cgb_mag_extended_source_grad")
     return _out(mag_out, was_np), _out(g, was_np)
+
+
+class BatchedLightCurves:
+    """Fixed-shape batched light-curve evaluator.  Buffers (times, offsets,
+    curve parameters, outputs and the work-queue workspace) are allocated once;
+    the launch sequence of mag_lc_batched (queue reset, per-point pass,
+    persistent contour kernel) is captured in a CUDA graph and replayed for new
+    curve parameters; the launch shape comes from the autotuner."""
+
+    def __init__(self, offsets, t, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
+                 precision="mixed", tune=True, graph=True, curves_for_tuning=None, config=None):
+        from . import autotune
+        self.offsets, _ = _to_device(offsets, torch.int64)
+        self.t, _ = _to_device(t, torch.float64)
+        dev = self.t.device
+        n = self.t.numel()
+        self.curves = torch.zeros((self.offsets.numel() - 1, 8), dtype=torch.float64, device=dev)
+        self.mag = torch.empty(n, dtype=torch.float64, device=dev)
+        self.route = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.status = torch.zeros(n, dtype=torch.int32, device=dev)
+        self.ws, _ = _workspace(n, dev)
+        self.kw = dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=roots_itmax,
+                       precision=precision)
+        if config is None:
+            config = (autotune.tune(self.offsets, self.t, curves_for_tuning, **self.kw)
+                      if tune and curves_for_tuning is not None else autotune.DEFAULT)
+        self.config = dict(config)
+        self.graph, self.graph_error = None, None
+        if graph:
+            if curves_for_tuning is not None:
+                self.curves.copy_(torch.as_tensor(np.asarray(curves_for_tuning)) if not isinstance(
+                    curves_for_tuning, torch.Tensor) else curves_for_tuning)
+            side = torch.cuda.Stream(device=dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(side):
+                self._launch()  # warm-up outside capture (sets kernel attributes)
+            torch.cuda.current_stream(dev).wait_stream(side)
+            self.graph = torch.cuda.CUDAGraph()
+            try:
+                with torch.cuda.graph(self.graph):
+                    self._launch()
+            except RuntimeError as e:  # capture refused: eager launches of the same kernels
+                self.graph, self.graph_error = None, str(e)
+
+    def _launch(self):
+        return mag_lc_batched(self.offsets, self.t, self.curves, out=(self.mag, self.route, self.status, self.ws),
+                              **self.kw, **self.config)
+
+    def __call__(self, curves):
+        """Magnifications for curve parameters [ncurves, 8]; returns the
+        evaluator's output tensor (overwritten by the next call)."""
+        self.curves.copy_(curves if isinstance(curves, torch.Tensor) else torch.as_tensor(np.asarray(curves)))
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch()
+        return self.mag

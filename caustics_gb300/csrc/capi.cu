@@ -107,6 +107,8 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
   P.CPcap = deg * (P.Lcap + 1) + 8;
   P.ld = o->limb_darkening ? 1 : 0;
   P.itmax = o->roots_itmax > 0 ? o->roots_itmax : 2500;
+  P.ld_group = (o->ld_group == 2 || o->ld_group == 4 || o->ld_group == 8) ? o->ld_group : 1;
+  P.qchunk = o->queue_chunk > 0 ? o->queue_chunk : 1;
   if (P.ld) {
     P.n1 = o->npts_ld / 2;
     P.n2 = o->npts_ld - P.n1;

@@ -561,7 +561,7 @@ __device__ __forceinline__ double split_point(double a, double b, double rho) {
 // each split at the reference's split point into two Gauss-Legendre pieces.
 // The node loop is uniform across the warp, so node tables are broadcast.
 template <int NL>
-__device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0) {
+__device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0, int j0, int jstep) {
   const double c0 = 3.0 / (3.0 - It.u1), u1 = It.u1, inv_rho = 1.0 / It.rho;
   const cd w0 = It.w0;
   double acc[2] = {0.0, 0.0};
@@ -575,7 +575,7 @@ __device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0) {
       const double hw = 0.5 * (hi - lo), mid = 0.5 * (hi + lo);
       const int n = half ? P.n2 : P.n1;
       double sum = 0.0;
-      for (int j = 0; j < n; ++j) {
+      for (int j = j0; j < n; j += jstep) {
         const double xn = fma(hw, P.gl_x[half][j], mid);
         cd zn = isQ ? mk(xn, zc.y) : mk(zc.x, xn);
         double r = cabs(lens_eq<NL>(It.L, zn) - w0) * inv_rho;
@@ -594,7 +594,7 @@ __device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0) {
 // the FP64 prologue (once per point) provides every difference, so each FP32
 // quantity is small relative to its own scale.
 template <int NL>
-__device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0) {
+__device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0, int j0, int jstep) {
   const float c0 = (float)(3.0 / (3.0 - It.u1)), u1 = (float)It.u1;
   const double inv_rho = 1.0 / It.rho;
   const cf uc = tof((lens_eq<NL>(It.L, zc) - It.w0) * inv_rho);
@@ -620,7 +620,7 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0) 
       const float hw = 0.5f * (hi_r - lo_r), mid = 0.5f * (hi_r + lo_r);
       const int n = half ? P.n2 : P.n1;
       float sum = 0.0f;
-      for (int j = 0; j < n; ++j) {
+      for (int j = j0; j < n; j += jstep) {
         const float d = fmaf(hw, (float)P.gl_x[half][j], mid);
         // delta = d (Q, along x) or i d (P, along y); conj(delta) = d or -i d
         const cf cdl = isQ ? mkf(d, 0.0f) : mkf(0.0f, -d);
@@ -697,6 +697,10 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
   }
   const R irho = (R)inv_rho, u1 = (R)It.u1;
   const R c0 = (R)(3.0 / (3.0 - It.u1)), dc0 = (R)(3.0 / ((3.0 - It.u1) * (3.0 - It.u1)));
+  // 1 - |s/rho|^2 = (1 - |uc|^2) - 2 Re(conj(uc) dl) - |dl|^2 with the first
+  // term in FP64: dB/dr ~ 1/sqrt(1 - r^2) near the limb, so 1 - r^2 must carry
+  // an error relative to itself, not the rounding of r.
+  const R c1 = (R)(1.0 - (uc64.x * uc64.x + uc64.y * uc64.y));
 #pragma unroll
   for (int isQ = 0; isQ < 2; ++isQ) {
     const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
@@ -715,25 +719,26 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         const R d = hw * t + mid;
         const C cdl = isQ ? C{d, (R)0} : C{(R)0, -d};  // conj(delta)
         // s/rho = uc + delta/rho + sum eps conj(delta) / (D (D + conj(delta))) / rho
-        C srho = isQ ? C{uc.x + d * irho, uc.y} : C{uc.x, uc.y + d * irho};
+        C dl = isQ ? C{d * irho, (R)0} : C{(R)0, d * irho};
         C u[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
           u[k] = crecip(Dj[k] + cdl);
-          srho = srho + cdl * u[k] * iDj[k] * (ej[k] * irho);
+          dl = dl + cdl * u[k] * iDj[k] * (ej[k] * irho);
         }
+        const C srho = C{uc.x + dl.x, uc.y + dl.y};
+        const R x1 = c1 - (R)2 * (uc.x * dl.x + uc.y * dl.y) - (dl.x * dl.x + dl.y * dl.y);  // 1 - r^2
         const R r = cabs(srho);
         R B, dB;
-        if (r <= (R)1) {
-          const R x = (R)1 - r * r;
-          const R sq = x > (R)0 ? sqrt(x) : (R)0;
+        if (x1 >= (R)0) {
+          const R sq = sqrt(x1);
           B = (R)1 + sq;
-          dB = x > (R)0 ? -r / sq : (R)0;
+          dB = x1 > (R)0 ? -r / sq : (R)0;
         } else {
-          const R x = (R)1 - (R)1 / (r * r);
-          const R sq = x > (R)0 ? sqrt(x) : (R)0;
+          const R r2 = r * r, x = -x1 / r2;  // 1 - 1/r^2
+          const R sq = sqrt(x);
           B = (R)1 - sq;
-          dB = x > (R)0 ? -(R)1 / (r * r * r * sq) : (R)0;
+          dB = -(R)1 / (r2 * r * sq);
         }
         const R I = c0 * (u1 * B + (R)1 - (R)2 * u1);
         const R dIdr = c0 * u1 * dB;
@@ -1400,17 +1405,34 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     }
     __syncthreads();
     if (P.ld) {
-      // one thread per contour point: I_c = sum_i P_i wx_i + Q_i wy_i (trapezoid weights)
+      // groups of G lanes per contour point (G = P.ld_group), each lane taking
+      // every G-th node: I_c = sum_i P_i wx_i + Q_i wy_i (trapezoid weights)
+      const int G = P.ld_group, groups = ES_THREADS / G, r = tid % G, gid = tid / G;
+      const int iters = (ntot + groups - 1) / groups;
       int c = 0;
-      for (int i = tid; i < ntot; i += ES_THREADS) {
-        while (i >= cstart[c + 1]) ++c;
-        const int b = cstart[c], e = min(cstart[c + 1], ntot);
-        cd zc = S.Z[S.CP[i]];
-        cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
-        double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
-        cd pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, zc, centroid[c]) : ld_point_fp64<NL>(P, I, zc, centroid[c]);
-        if (GRAD) S.PQ[i] = pq;
-        atomicAdd(&contour_acc[warp][c], pq.x * wx + pq.y * wy);
+      for (int it = 0; it < iters; ++it) {
+        const int i = it * groups + gid;
+        const bool valid = i < ntot;
+        cd pq = mk(0, 0);
+        double wx = 0.0, wy = 0.0;
+        if (valid) {
+          while (i >= cstart[c + 1]) ++c;
+          const int b = cstart[c], e = min(cstart[c + 1], ntot);
+          cd zc = S.Z[S.CP[i]];
+          cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
+          wx = 0.5 * (zn.x - zp.x);
+          wy = 0.5 * (zn.y - zp.y);
+          pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, zc, centroid[c], r, G)
+                               : ld_point_fp64<NL>(P, I, zc, centroid[c], r, G);
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) {
+          pq.x += __shfl_xor_sync(0xffffffffu, pq.x, o);
+          pq.y += __shfl_xor_sync(0xffffffffu, pq.y, o);
+        }
+        if (valid && r == 0) {
+          if (GRAD) S.PQ[i] = pq;
+          atomicAdd(&contour_acc[warp][c], pq.x * wx + pq.y * wy);
+        }
       }
     } else {
       // uniform: 1/2 sum (x_i + x_{i+1})/2 (y_{i+1} - y_i) - (y_i + y_{i+1})/2 (x_{i+1} - x_i)

@@ -60,6 +60,7 @@ typedef struct cgb_es_options {
   int32_t precision;      /* CGB_PREC_FP64 or CGB_PREC_MIXED */
   int32_t grid;           /* CTAs to launch, 0 = automatic */
   int32_t queue_chunk;    /* batched light curves: work items taken per queue grab (>= 1) */
+  int32_t ld_group;       /* lanes sharing one contour point's quadrature nodes: 1, 2, 4 or 8 */
 } cgb_es_options;
 
 /* Parameters of one binary-lens light curve for the batched entry points: lens

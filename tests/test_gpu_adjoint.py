@@ -113,12 +113,20 @@ def test_adjoint_vs_central_differences(G, case, prec):
     assert checked >= 6 * len(w) // 2
 
 
-def test_adjoint_vs_oracle_frozen_structure(G):
+@pytest.mark.parametrize("prec", [0, 1])
+def test_adjoint_vs_oracle_frozen_structure(G, prec):
     """Against the oracle's frozen-structure finite differences (the smooth
-    function autodiff differentiates), steps 1e-8 relative."""
+    function autodiff differentiates).  Limb points within ~1e-7 of a caustic
+    keep the difference quotient curved down to steps of 1e-8, so a component
+    counts only where the steps 1e-8 and 1e-9 (relative) agree to 5e-4."""
     d = G("mag_es4")
+    checked = 0
     for w in d["w"][:3]:
-        mag, g = grad(np.array([w]), 1e-2, 0.9, 0.2, 0.7, 300, 100, True, 0)
-        ref = O.frozen_gradient(w, 1e-2, 0.9, 0.2, 300, True, 0.7, 100, rel=1e-8)
-        scale = np.maximum(np.abs(ref), 1e-3 * mag[0])
-        assert np.all(np.abs(g[0] - ref) / scale < 2e-3), (g[0], ref)
+        mag, g = grad(np.array([w]), 1e-2, 0.9, 0.2, 0.7, 300, 100, True, prec)
+        r1 = O.frozen_gradient(w, 1e-2, 0.9, 0.2, 300, True, 0.7, 100, rel=1e-8)
+        r2 = O.frozen_gradient(w, 1e-2, 0.9, 0.2, 300, True, 0.7, 100, rel=1e-9)
+        scale = np.maximum(np.abs(r2), 1e-3 * mag[0])
+        ok = np.abs(r1 - r2) <= 5e-4 * scale
+        assert np.all(np.abs(g[0] - r2)[ok] / scale[ok] < 2e-3), (g[0], r2, ok)
+        checked += ok.sum()
+    assert checked >= 12
