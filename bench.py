@@ -260,32 +260,59 @@ def extras_triple(C, dev, stream, nsys=1000, per_sys=1000, big=1 << 20):
     """Triple-lens point source, mixed (FP32 Aberth + compensated double-float
     Horner + FP64 polish) against FP64: 1000 systems x 1000 positions (seed 1,
     s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4, 1e-1], psi ~ U[0, 2pi];
-    s = s1, q = q1, q3 = q2, r3 = s2).  Throughput from one 2^20-position call."""
+    s = s1, q = q1, q3 = q2, r3 = s2).  Image counts compared per point (the two
+    solvers order roots differently), excluding points whose residual sits within
+    x30 of the reference's 1e-6 image threshold.  Throughput from one
+    2^20-position call on a system the mixed solver handles.""" 
     import torch
     rng = np.random.default_rng(1)
     sysp = np.stack([rng.uniform(0.5, 2, nsys), rng.uniform(0.5, 2, nsys), 10 ** rng.uniform(-4, 0, nsys),
                      10 ** rng.uniform(-4, -1, nsys), rng.uniform(0, 2 * np.pi, nsys)], axis=1)
     w = rng.uniform(-1.5, 1.5, (nsys, per_sys)) + 1j * rng.uniform(-1.5, 1.5, (nsys, per_sys))
     wd = torch.as_tensor(w, device=dev)
-    maxerr, count_mismatch, root_err = 0.0, 0, 0.0
+    maxerr, maxerr_clear, mismatch, ambiguous, fallback, root_err = 0.0, 0.0, 0, 0, 0, []
+
+    def popcount(x):
+        x = x.to(torch.int64)
+        return sum(((x >> b) & 1) for b in range(10))
     for k in range(nsys):
         p = dict(s=sysp[k, 0], q=sysp[k, 2], q3=sysp[k, 3], r3=sysp[k, 1], psi=sysp[k, 4])
-        m64, z64, k64 = C.mag_point_source(wd[k], nlenses=3, precision="fp64", return_images=True, **p)
-        m32, z32, k32 = C.mag_point_source(wd[k], nlenses=3, precision="mixed", return_images=True, **p)
-        maxerr = max(maxerr, float((torch.abs(m32 - m64) / m64).max().item()))
-        count_mismatch += int((k32 != k64).sum().item())
-        d = torch.abs(z32[:, :, None] - z64[:, None, :]).min(dim=2).values / torch.clamp(torch.abs(z64), min=1e-300)
-        root_err = max(root_err, float(d.max().item()))
-    p = dict(s=sysp[0, 0], q=sysp[0, 2], q3=sysp[0, 3], r3=sysp[0, 1], psi=sysp[0, 4])
+        m64, z64, k64, s64 = C.mag_point_source(wd[k], nlenses=3, precision="fp64", return_images=True,
+                                                return_status=True, **p)
+        m32, z32, k32, s32 = C.mag_point_source(wd[k], nlenses=3, precision="mixed", return_images=True,
+                                                return_status=True, **p)
+        rel = torch.abs(m32 - m64) / m64
+        amb = ((s64 | s32) & 2) != 0  # residual within x30 of the reference's 1e-6 image threshold
+        maxerr = max(maxerr, float(rel.max().item()))
+        if (~amb).any():
+            maxerr_clear = max(maxerr_clear, float(rel[~amb].max().item()))
+        mismatch += int(((popcount(k32) != popcount(k64)) & ~amb).sum().item())
+        ambiguous += int(amb.sum().item())
+        fallback += int(((s32 & 4) != 0).sum().item())
+        # roots as sets: distance of each FP64 root to the nearest mixed root, relative to max(|z|, 1)
+        d = torch.abs(z64[:, :, None] - z32[:, None, :]).min(dim=2).values / torch.clamp(torch.abs(z64), min=1.0)
+        root_err.append(d.reshape(-1))
+    root_err = torch.cat(root_err)
+    # throughput on the first system whose mass fractions all reach 1e-2 (below
+    # that the mixed path hands triple lenses to the FP64 solver)
+    e1 = sysp[:, 2] / (1 + sysp[:, 2] + sysp[:, 3])
+    e2 = sysp[:, 2] * e1
+    k0 = int(np.flatnonzero(np.minimum(np.minimum(e1, e2), 1 - e1 - e2) >= 1e-2)[0])
+    p = dict(s=sysp[k0, 0], q=sysp[k0, 2], q3=sysp[k0, 3], r3=sysp[k0, 1], psi=sysp[k0, 4])
     wb = torch.as_tensor(rng.uniform(-1.5, 1.5, big) + 1j * rng.uniform(-1.5, 1.5, big), device=dev)
     rate = {}
     for prec in ("fp64", "mixed"):
         C.mag_point_source(wb, nlenses=3, precision=prec, **p)
         rate[prec] = big / (timed(stream, lambda: C.mag_point_source(wb, nlenses=3, precision=prec, **p), 3) * 1e-3)
-    return {"workload": "1000 systems x 1000 positions, seed 1 (throughput: 2^20 positions of system 0)",
+    return {"workload": f"1000 systems x 1000 positions, seed 1 (throughput: 2^20 positions of system {k0})",
+            "systems_on_fp64_solver": int((np.minimum(np.minimum(e1, e2), 1 - e1 - e2) < 1e-2).sum()),
             "fp64_evals_per_s": rate["fp64"], "mixed_evals_per_s": rate["mixed"],
-            "mixed_vs_fp64_max_rel_mag_err": maxerr, "image_count_mismatches": count_mismatch,
-            "max_rel_root_err": root_err}
+            "mixed_vs_fp64_max_rel_mag_err": maxerr, "mixed_vs_fp64_max_rel_mag_err_unambiguous": maxerr_clear,
+            "image_count_mismatches_unambiguous": mismatch, "ambiguous_points": ambiguous,
+            "mixed_fp64_fallbacks": fallback,
+            "root_err_vs_fp64": {"median": float(root_err.median().item()),
+                                 "p99": float(torch.quantile(root_err[:1 << 20], 0.99).item()),
+                                 "max": float(root_err.max().item())}}
 
 
 def main():

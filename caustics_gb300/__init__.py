@@ -16,7 +16,10 @@ from .api import (  # noqa: F401
     mag_extended_source,
     mag_point_source,
     poly_roots,
+    roots_jvp,
+    roots_vjp,
 )
 
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
-           "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves"]
+           "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves",
+           "roots_jvp", "roots_vjp"]

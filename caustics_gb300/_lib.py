@@ -50,6 +50,8 @@ SIGNATURES = {
     "cgb_gauss_legendre": (ctypes.c_int, [ctypes.c_int32, _P, _P]),
     "cgb_ea_solve": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "gpu_ehrlich_aberth": (None, [_P, _P, ctypes.c_char_p, ctypes.c_size_t]),
+    "cgb_ea_roots_jvp": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, _P]),
+    "cgb_ea_roots_vjp": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P]),
     "cgb_mag_point_source": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, LensParams, ctypes.c_int32,
                                             ctypes.c_int32, _P, _P]),
     "cgb_mag_extended_source": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, LensParams,

@@ -66,23 +66,85 @@ def _precision(p):
 # root solver primitive
 # ---------------------------------------------------------------------------
 
+def _solve(c, ri, itmax, prec, status):
+    m, n1 = c.shape
+    roots = torch.empty((m, n1 - 1), dtype=torch.complex128, device=c.device)
+    with torch.cuda.device(c.device):
+        L.check(L.lib().cgb_ea_solve(_ptr(c), _ptr(ri), _ptr(roots), m, n1 - 1, int(itmax or 2000), prec,
+                                     _ptr(status), _stream()), "cgb_ea_solve")
+    return roots
+
+
+class _Roots(torch.autograd.Function):
+    """Roots with the implicit-function rule as backward
+    (ehrlich_aberth_primitive.py:252-312; torch's conjugate convention)."""
+
+    @staticmethod
+    def forward(ctx, c, ri, itmax, prec, status):
+        roots = _solve(c, ri, itmax, prec, status)
+        ctx.save_for_backward(c, roots)
+        return roots
+
+    @staticmethod
+    def backward(ctx, g):
+        c, roots = ctx.saved_tensors
+        ct = torch.empty_like(c)
+        g = g.contiguous()
+        with torch.cuda.device(c.device):
+            L.check(L.lib().cgb_ea_roots_vjp(_ptr(c), _ptr(roots), _ptr(g), _ptr(ct), c.shape[0], c.shape[1] - 1, 1,
+                                             _stream()), "cgb_ea_roots_vjp")
+        return ct, None, None, None, None
+
+
 def ehrlich_aberth(coeffs, roots_init, itmax=None, compensated=None, custom_init=False, precision=None, status=None):
     """Batched primitive: coeffs complex128 [M, deg+1] low->high, roots_init
-    [M, deg]; returns roots [M*deg] (ehrlich_aberth_primitive.py:98-106)."""
+    [M, deg]; returns roots [M*deg] (ehrlich_aberth_primitive.py:98-106).
+    Differentiable with respect to coeffs (torch autograd)."""
     c, was_np = _to_device(coeffs, torch.complex128)
     m, n1 = c.shape
     deg = n1 - 1
-    roots = torch.empty((m, deg), dtype=torch.complex128, device=c.device)
     ri = None
     if custom_init:
         ri, _ = _to_device(roots_init, torch.complex128)
         ri = ri.reshape(m, deg).contiguous()
     prec = _precision(precision) if precision else (L.PREC_FP64_COMP if compensated else L.PREC_FP64)
-    st = status if status is not None else None
-    with torch.cuda.device(c.device):
-        L.check(L.lib().cgb_ea_solve(_ptr(c), _ptr(ri), _ptr(roots), m, deg, int(itmax or 2000), prec, _ptr(st),
-                                     _stream()), "cgb_ea_solve")
+    if c.requires_grad:
+        roots = _Roots.apply(c, ri, itmax, prec, status)
+    else:
+        roots = _solve(c, ri, itmax, prec, status)
     return _out(roots.reshape(-1), was_np)
+
+
+def roots_jvp(coeffs, roots, dcoeffs):
+    """Forward-mode derivative of the roots (the primitive's JVP rule,
+    ehrlich_aberth_primitive.py:252-312): coeffs, dcoeffs [M, deg+1] low->high,
+    roots [M, deg] -> droots [M, deg]."""
+    c, was_np = _to_device(coeffs, torch.complex128)
+    z, _ = _to_device(roots, torch.complex128)
+    dc, _ = _to_device(dcoeffs, torch.complex128)
+    m, n1 = c.shape
+    z = z.reshape(m, n1 - 1).contiguous()
+    dz = torch.empty_like(z)
+    with torch.cuda.device(c.device):
+        L.check(L.lib().cgb_ea_roots_jvp(_ptr(c), _ptr(z), _ptr(dc.reshape(m, n1).contiguous()), _ptr(dz), m, n1 - 1,
+                                         _stream()), "cgb_ea_roots_jvp")
+    return _out(dz, was_np)
+
+
+def roots_vjp(coeffs, roots, ct_roots, conjugate=False):
+    """Reverse-mode derivative of the roots: ct_roots [M, deg] -> ct_coeffs
+    [M, deg+1], the transpose of roots_jvp's map (conjugate transpose when
+    conjugate=True)."""
+    c, was_np = _to_device(coeffs, torch.complex128)
+    z, _ = _to_device(roots, torch.complex128)
+    ct, _ = _to_device(ct_roots, torch.complex128)
+    m, n1 = c.shape
+    out = torch.empty_like(c)
+    with torch.cuda.device(c.device):
+        L.check(L.lib().cgb_ea_roots_vjp(_ptr(c), _ptr(z.reshape(m, n1 - 1).contiguous()),
+                                         _ptr(ct.reshape(m, n1 - 1).contiguous()), _ptr(out), m, n1 - 1,
+                                         int(bool(conjugate)), _stream()), "cgb_ea_roots_vjp")
+    return _out(out, was_np)
 
 
 def poly_roots(coeffs, itmax=2000, compensated=False, custom_init=False, roots_init=None, precision=None):

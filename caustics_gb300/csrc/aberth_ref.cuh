@@ -117,4 +117,85 @@ __device__ int solve(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm)
   return -1;
 }
 
+// The same iteration spread over a group of G lanes (G a power of two >= DEG,
+// G <= 32; every lane of the group calls it together): lane r owns root r.
+// Root j's Horner values and stopping test depend on z_j alone, which nothing
+// changes before root j's own update, so all roots are evaluated at the start
+// of an iteration; then, for j in order, the terms 1/(z_j - z_i) are formed on
+// lanes i and summed in the serial order, and lane j applies its correction.
+// The arithmetic of every value is that of solve(), so the iterates are the same
+// bit for bit, at about a quarter of the sequential FP64 instructions.
+template <int G>
+__device__ __forceinline__ cd gshfl(unsigned mask, cd v, int src) {
+  return cd{__shfl_sync(mask, v.x, src, G), __shfl_sync(mask, v.y, src, G)};
+}
+
+template <int DEG, int G>
+__device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm) {
+  static_assert(G >= DEG && G <= 32 && (G & (G - 1)) == 0, "group size");
+  const int lane = threadIdx.x & 31, r = lane & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
+  double alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = absc(p[i]);
+  if (!warm) {
+    cd t[DEG];
+    init_real<DEG>(alpha, t);
+    zr = cd{0.0, 0.0};
+#pragma unroll
+    for (int i = 0; i < DEG; ++i)
+      if (i == r) zr = t[i];
+  }
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = __dmul_rn(alpha[i], fma(3.8284271247461900976, (double)i, 1.0));
+  uint32_t conv = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  const double EPS = 1.1102230246251565e-16;
+  for (int it = 0; it < itmax; ++it) {
+    bool stop = false, rev = false;
+    cd h = cd{0.0, 0.0}, hd = cd{0.0, 0.0};
+    if (r < DEG && !((conv >> r) & 1u)) {
+      double az = absc(zr);
+      rev = az > 1.0;
+      cd x = rev ? recip(zr) : zr;
+      double ax = rev ? __ddiv_rn(1.0, az) : az;
+      double b = rev ? alpha[0] : alpha[DEG];
+      h = rev ? p[0] : p[DEG];
+#pragma unroll
+      for (int k = 1; k <= DEG; ++k) {
+        b = fma(b, ax, rev ? alpha[k] : alpha[DEG - k]);
+        hd = add(mul(hd, x), h);
+        h = add(mul(h, x), rev ? p[k] : p[DEG - k]);
+      }
+      stop = !(absc(h) > __dmul_rn(EPS, b));
+    }
+    const uint32_t newly = (__ballot_sync(gmask, stop) >> (lane - r)) & all;
+    for (int j = 0; j < DEG; ++j) {
+      if (((conv | newly) >> j) & 1u) continue;  // uniform over the group
+      const cd zj = gshfl<G>(gmask, zr, j);
+      cd term = cd{0.0, 0.0};
+      if (r < DEG && r != j) term = recip(sub(zj, zr));
+      cd s = cd{0.0, 0.0};
+#pragma unroll
+      for (int i = 0; i < DEG; ++i) {
+        const cd ti = gshfl<G>(gmask, term, i);
+        if (i != j) s = add(s, ti);
+      }
+      if (r == j) {
+        cd corr;
+        if (rev) {
+          cd z2h = mul(sq_pow(zr), h);
+          corr = div(z2h, sub(sub(scale(mul(zr, h), (double)DEG), hd), mul(z2h, s)));
+        } else {
+          corr = div(h, sub(hd, mul(h, s)));
+        }
+        zr = sub(zr, corr);
+      }
+    }
+    conv |= newly;
+    if (conv == all) return it + 1;
+  }
+  return -1;
+}
+
 }  // namespace refea

@@ -231,38 +231,58 @@ __device__ uint64_t step_map(const cd *a, const cd *b, bool &ambiguous) {
 // Which root of limb point k each root of point k-1 reaches when the reference
 // warm-starts point k from point k-1 with rows in order `prev` (track -> raw row
 // of k-1), computed with the reference's arithmetic (point_source.py:1711-1759,
-// extended_source.py:79-98).  jitter adds the warm-start perturbation of the
-// refinement solves.  Returns the map raw root of k-1 -> raw root of k.
+// extended_source.py:79-98): warm_map_ref_group.  jitter adds the warm-start
+// perturbation of the refinement solves.  Returns the map raw root of k-1 ->
+// raw root of k.  first_point_order_group labels the first limb point's roots
+// as the reference's cold start from its real-valued initial guesses produces
+// them: track t -> raw row.
+// Lanes that share one faithful solve (one lane per root).
+template <int DEG>
+struct RefGroup {
+  static constexpr int G = DEG <= 8 ? 8 : 16;
+};
+
+// warm_map_ref / first_point_order on a group of RefGroup<DEG>::G lanes that
+// call together (refea::solve_group); every lane returns the map.
 template <int NL>
-__device__ uint64_t warm_map_ref(const EsParams &P, const EsItem &I, double th, const cd *zprev, uint64_t prev,
-                                 const cd *zcur, bool jitter) {
-  constexpr int DEG = NL * NL + 1;
+__device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, double th, const cd *zprev, uint64_t prev,
+                                       const cd *zcur, bool jitter) {
+  constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G;
+  const int lane = threadIdx.x & 31, r = lane & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
   double s, c;
   sincos(th, &s, &c);
-  cd p[DEG + 1], z[DEG];
+  cd p[DEG + 1];
   lens_poly<NL>(I.L, mk(__dadd_rn(__dmul_rn(I.rho, c), I.w0.x), __dadd_rn(__dmul_rn(I.rho, s), I.w0.y)), p);
-#pragma unroll
-  for (int t = 0; t < DEG; ++t) {
-    z[t] = zprev[perm_get(prev, t)];
-    if (jitter) z[t] = z[t] + mk(1e-6 * ((t & 1) ? 0.5 : -0.5), 1e-6 * ((t & 2) ? 0.5 : -0.5));
+  cd zr = mk(0.0, 0.0);
+  if (r < DEG) {
+    zr = zprev[perm_get(prev, r)];
+    if (jitter) zr = zr + mk(1e-6 * ((r & 1) ? 0.5 : -0.5), 1e-6 * ((r & 2) ? 0.5 : -0.5));
   }
-  refea::solve<DEG>(p, z, P.itmax, true);
-  uint64_t rowmap = greedy_match<DEG>(z, zcur);  // iterate t -> raw root of k
+  refea::solve_group<DEG, G>(p, zr, P.itmax, true);
+  cd z[DEG];
+#pragma unroll
+  for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
+  const uint64_t rowmap = greedy_match<DEG>(z, zcur);  // iterate t -> raw root of k
   uint64_t nb = 0;
   for (int t = 0; t < DEG; ++t) nb = perm_set(nb, perm_get(prev, t), perm_get(rowmap, t));
   return nb;
 }
 
-// Labelling of the first limb point's roots as the reference's cold start from
-// its real-valued initial guesses produces it: track t -> raw row.
 template <int NL>
-__device__ uint64_t first_point_order(const EsParams &P, const EsItem &I, double th, const cd *zraw) {
-  constexpr int DEG = NL * NL + 1;
+__device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, double th, const cd *zraw) {
+  constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G;
+  const int lane = threadIdx.x & 31, r = lane & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
   double s, c;
   sincos(th, &s, &c);
-  cd p[DEG + 1], z[DEG];
+  cd p[DEG + 1];
   lens_poly<NL>(I.L, mk(__dadd_rn(__dmul_rn(I.rho, c), I.w0.x), __dadd_rn(__dmul_rn(I.rho, s), I.w0.y)), p);
-  refea::solve<DEG>(p, z, P.itmax, false);
+  cd zr = mk(0.0, 0.0);
+  refea::solve_group<DEG, G>(p, zr, P.itmax, false);
+  cd z[DEG];
+#pragma unroll
+  for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
   return greedy_match<DEG>(z, zraw);
 }
 
@@ -796,6 +816,22 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
 }
 
 
+// Tangents dz/dtheta of a binary-lens image z on the limb point of angle th,
+// for theta = (rho, u1, Re w0, Im w0, a, e1): from lens_eq(z) = w0 + rho e^{i th},
+// dz = (g - lam conj(g)) / (1 - |lam|^2), lam = sum_j eps_j / (conj(z) - r_j)^2,
+// g = the source-plane shift the parameter produces at fixed z.
+__device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th, cd t[6]) {
+  const cd u0 = crecip(conj(z) - I.L.r[0]), u1 = crecip(conj(z) - I.L.r[1]);
+  const cd lam = u0 * u0 * I.L.eps[0] + u1 * u1 * I.L.eps[1];
+  const double iD = 1.0 / (1.0 - norm2(lam));
+  double sn, cs;
+  sincos(th, &sn, &cs);
+  const cd g[6] = {mk(cs, sn), mk(0.0, 0.0), mk(1.0, 0.0), mk(0.0, 1.0),
+                   u0 * u0 * I.L.eps[0] - u1 * u1 * I.L.eps[1], u0 - u1};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) t[k] = (g[k] - lam * conj(g[k])) * iD;
+}
+
 // Backward pass of one extended-source evaluation (binary lenses): the
 // contours of the forward pass are recomputed, never stored between passes.
 // T = sum_c parity_c I_c, mu = |T| / (pi rho^2).
@@ -837,11 +873,19 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
         const cd pq = S.PQ[i];
         atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
         atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
-        // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2
-        atomicAdd(&S.GG[in].x, 0.5 * pc * pq.x);
-        atomicAdd(&S.GG[ip].x, -0.5 * pc * pq.x);
-        atomicAdd(&S.GG[in].y, 0.5 * pc * pq.y);
-        atomicAdd(&S.GG[ip].y, -0.5 * pc * pq.y);
+        // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2, so P_i wx_i + Q_i wy_i
+        // contributes P_i (t_in - t_ip).x / 2 + Q_i (t_in - t_ip).y / 2 per
+        // parameter.  Summed by parts against the FP64 image tangents rather than
+        // scattered into the neighbours' position adjoints, where it would become
+        // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
+        // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
+        cd tn[6], tp[6];
+        const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
+        image_tangents(I, zn, S.TH[cpn / DEG], tn);
+        image_tangents(I, zp, S.TH[cpp / DEG], tp);
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+          acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
         atomicAdd(&cgr[c][1], pc * wx * g.Pa);
         atomicAdd(&cgr[c][0], pc * wy * g.Qa);
 #pragma unroll
@@ -878,21 +922,10 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
         G = G + mk(cgr[c][0] * inv_n, cgr[c][1] * inv_n);
       }
       const uint32_t cp = S.CP[i];
-      const cd z = S.Z[cp];
-      const double th = S.TH[cp / DEG];
-      const cd u0 = crecip(conj(z) - I.L.r[0]), u1 = crecip(conj(z) - I.L.r[1]);
-      const cd lam = u0 * u0 * I.L.eps[0] + u1 * u1 * I.L.eps[1];
-      const double D = 1.0 - norm2(lam);
-      const cd H = cdiv(conj(G) - G * conj(lam), mk(D, 0.0));
-      const cd fa = u0 * u0 * I.L.eps[0] - u1 * u1 * I.L.eps[1];
-      const cd fe = u0 - u1;
-      double sn, cs;
-      sincos(th, &sn, &cs);
-      acc[GK_WX] += H.x;
-      acc[GK_WY] += -H.y;
-      acc[GK_RHO] += H.x * cs - H.y * sn;
-      acc[GK_A] += H.x * fa.x - H.y * fa.y;
-      acc[GK_E1] += H.x * fe.x - H.y * fe.y;
+      cd t[6];
+      image_tangents(I, S.Z[cp], S.TH[cp / DEG], t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) acc[k] += G.x * t[k].x + G.y * t[k].y;
     }
   }
 #pragma unroll
@@ -961,6 +994,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   __shared__ int cpar[MAX_CLOSED + N_CONTOURS];
   __shared__ uint32_t sflags;
   __shared__ int nsel_sh;
+  __shared__ int nlist_sh;
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
   __shared__ EsItem item;
@@ -1088,7 +1122,11 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     // parallel: clear steps take the nearest-root map; ambiguous steps rerun the
     // reference's warm start from the predecessor in the current chain order,
     // and the chain is recomposed until no ambiguous map moves.
-    if (tid == 0) S.PERM[0] = first_point_order<NL>(P, I, S.TH[0], S.Z);
+    constexpr int RG = RefGroup<DEG>::G;
+    if (tid < RG) {
+      const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z);
+      if (tid == 0) S.PERM[0] = o;
+    }
     for (int k = 1 + tid; k < n0; k += ES_THREADS) {
       bool amb;
       S.BMAP[k] = step_map<DEG>(S.Z + (size_t)(k - 1) * DEG, S.Z + (size_t)k * DEG, amb);
@@ -1105,21 +1143,32 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           ord = nw;
         }
         nsel_sh = 0;
+        nlist_sh = 0;
       }
       __syncthreads();
       if (round == 11) {
         if (tid == 0) atomicOr(&sflags, CGB_ST_MERGE);
         break;
       }
+      // steps whose map must be (re)computed from the current chain order
       for (int k = 1 + tid; k < n0; k += ES_THREADS) {
         const uint64_t prev = S.PERM[k - 1], used = S.USED[k];
         if (used == 0ull || used == prev) continue;
-        uint64_t nb = warm_map_ref<NL>(P, I, S.TH[k], S.Z + (size_t)(k - 1) * DEG, prev, S.Z + (size_t)k * DEG, false);
-        if (nb != S.BMAP[k]) {
-          S.BMAP[k] = nb;
-          nsel_sh = 1;
+        S.SCAN[atomicAdd(&nlist_sh, 1)] = k;
+      }
+      __syncthreads();
+      for (int e = tid / RG; e < nlist_sh; e += ES_THREADS / RG) {
+        const int k = S.SCAN[e];
+        const uint64_t prev = S.PERM[k - 1];
+        const uint64_t nb =
+            warm_map_ref_group<NL>(P, I, S.TH[k], S.Z + (size_t)(k - 1) * DEG, prev, S.Z + (size_t)k * DEG, false);
+        if ((tid & (RG - 1)) == 0) {
+          if (nb != S.BMAP[k]) {
+            S.BMAP[k] = nb;
+            nsel_sh = 1;
+          }
+          S.USED[k] = prev;
         }
-        S.USED[k] = prev;
       }
       __syncthreads();
       const bool again = nsel_sh != 0;
@@ -1139,23 +1188,27 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
         const int s1 = S.ORD[k], s2 = S.ORD[k + 1];
         const cd *a = S.Z + (size_t)s1 * DEG, *b = S.Z + (size_t)s2 * DEG;
         const uint16_t m = S.MK[s1] | S.MK[s2];
-        double g = 0.0;
+        double g2 = 0.0;  // max |b - a| = sqrt(max |b - a|^2): sqrt is monotone and correctly rounded
         for (int i = 0; i < DEG; ++i)
-          if ((m >> i) & 1u) g = fmax(g, cabs(b[i] - a[i]));
-        S.KEY[k] = g;
+          if ((m >> i) & 1u) g2 = fmax(g2, norm2(b[i] - a[i]));
+        S.KEY[k] = sqrt(g2);
       }
       __syncthreads();
-      // rank: larger gap first, ties -> larger index first
+      // rank: larger gap first, ties -> larger index first.  Gaps are >= +0, so
+      // their IEEE bit patterns order as integers (integer pipe, not FP64).
       for (int k = tid; k < ngap; k += ES_THREADS) {
-        const double g = S.KEY[k];
+        const long long g = __double_as_longlong(S.KEY[k]);
         int rank = 0;
         for (int j = 0; j < ngap; ++j) {
-          double h = S.KEY[j];
+          const long long h = __double_as_longlong(S.KEY[j]);
           rank += (h > g) || (h == g && j > k);
         }
         S.SCAN[k] = rank < P.n_add ? 1 : 0;
       }
-      if (tid == 0) S.SCAN[ngap] = 0;
+      if (tid == 0) {
+        S.SCAN[ngap] = 0;
+        nlist_sh = 0;
+      }
       __syncthreads();
       // positions of the selected gaps -> compact list in SCAN (exclusive scan)
       for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
@@ -1174,13 +1227,22 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
                                      S.PP[slot], S.ZP[slot], flags);
           bool amb;
-          uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
-          if (amb) {
-            uint64_t ident = 0;
-            for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
-            m = warm_map_ref<NL>(P, I, th, S.Z + (size_t)sl * DEG, ident, S.Z + (size_t)slot * DEG, true);
-          }
-          apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+          const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
+          if (amb)  // labelled below by the reference's warm start, on a lane group
+            S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
+          else
+            apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+        }
+      }
+      __syncthreads();
+      {
+        uint64_t ident = 0;
+        for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
+        for (int e = tid / RG; e < nlist_sh; e += ES_THREADS / RG) {
+          const int slot = (int)(S.USED[e] & 0xffffu), sl = (int)((S.USED[e] >> 16) & 0xffffu);
+          const uint64_t m = warm_map_ref_group<NL>(P, I, S.TH[slot], S.Z + (size_t)sl * DEG, ident,
+                                                    S.Z + (size_t)slot * DEG, true);
+          if ((tid & (RG - 1)) == 0) apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
         }
       }
       __syncthreads();

@@ -12,6 +12,12 @@ enum Precision : int { FP64 = 0, MIXED = 1, FP64_COMP = 2 };
 cudaError_t launch_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int deg,
                             int itmax, int precision, uint32_t *status, cudaStream_t stream);
 
+// implicit-function JVP / VJP of polynomial roots (roots_ad.cu)
+cudaError_t launch_roots_jvp(const double *coeffs, const double *roots, const double *dcoeffs, double *droots,
+                             int64_t n, int deg, cudaStream_t stream);
+cudaError_t launch_roots_vjp(const double *coeffs, const double *roots, const double *ct_roots, double *ct_coeffs,
+                             int64_t n, int deg, int conjugate, cudaStream_t stream);
+
 cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *images, uint32_t *image_mask,
                           int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream);
 

@@ -92,6 +92,18 @@ int cgb_gauss_legendre(int32_t n, double *x, double *w);
 int cgb_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int32_t deg,
                  int32_t itmax, int32_t precision, uint32_t *status, void *stream);
 
+/* Implicit-function derivatives of the roots returned by cgb_ea_solve, the
+ * JVP rule of the reference's primitive (src/caustics/ehrlich_aberth_primitive.py:252-312):
+ * dz_r = -sum_k z_r^k dp_k / p'(z_r), coefficients low -> high.
+ * jvp: dcoeffs complex128[n, deg+1] -> droots complex128[n, deg].
+ * vjp: ct_roots complex128[n, deg] -> ct_coeffs complex128[n, deg+1], the
+ * transpose of the JVP map (conjugate = 0, JAX's convention) or its conjugate
+ * transpose (conjugate = 1, torch's convention for complex tensors). */
+int cgb_ea_roots_jvp(const double *coeffs, const double *roots, const double *dcoeffs, double *droots, int64_t n,
+                     int32_t deg, void *stream);
+int cgb_ea_roots_vjp(const double *coeffs, const double *roots, const double *ct_roots, double *ct_coeffs, int64_t n,
+                     int32_t deg, int32_t conjugate, void *stream);
+
 /* The reference's legacy XLA GPU custom-call signature with its opaque
  * descriptor {int size, deg, itmax; bool compensated}
  * (lib/ehrlich_aberth/kernels.h:11-20, gpu_ops.cc:14-25): buffers[0] = coeffs,

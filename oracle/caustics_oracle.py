@@ -95,6 +95,16 @@ def poly_roots(coeffs, itmax=2000, compensated=False, custom_init=False, roots_i
                     roots_init=roots_init if custom_init else None, init_mode=init_mode)
 
 
+def roots_jvp(p, z, dp):
+    """Implicit-function JVP of the roots (src/caustics/ehrlich_aberth_primitive.py:252-312):
+    p, dp [M, deg+1] low->high, z [M, deg] -> dz_r = -sum_k z_r^k dp_k / p'(z_r)."""
+    p, z, dp = (np.asarray(x, dtype=np.complex128) for x in (p, z, dp))
+    deg = p.shape[1] - 1
+    dfdz = np.stack([np.polyval(np.polyder(pi[::-1]), zi) for pi, zi in zip(p, z)])  # :292-293
+    dfdp = z[..., None] ** np.arange(deg + 1)  # [M, deg, deg+1], :301
+    return -np.einsum("mrk,mk->mr", dfdp, dp) / dfdz  # :304-307
+
+
 # ----------------------------------------------------------------------------
 # Lens configuration
 # ----------------------------------------------------------------------------

@@ -17,7 +17,7 @@ Known deviations of this harness from the reference under real JAX:
 * roots come from the reference's C++ solver through ctypes instead of an XLA
   custom call (identical code, compiled with g++ -O2 -DNDEBUG).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp]
 """
 import argparse
 import ctypes
@@ -98,12 +98,43 @@ def near_caustic_points(caustic, rho, n, seed):
     return c[idx] + r * np.exp(1j * phi)
 
 
+def roots_jvp_fixture(poly_roots, ps):
+    """Derivatives of the reference solver's roots along random coefficient
+    tangents, by central differences of the reference solver itself (step 1e-7
+    relative, roots matched to the unperturbed ones): the known answer for the
+    primitive's implicit-function JVP (ehrlich_aberth_primitive.py:252-312),
+    whose JAX evaluation is not available."""
+    rng = np.random.default_rng(21)
+    w = rng.uniform(-1.2, 1.2, 24) + 1j * rng.uniform(-1.2, 1.2, 24)
+    out = {}
+    polys = {"5": np.asarray(ps._poly_coeffs_binary(w, 0.45, 1 / 1.1))}
+    # a triple system without a tiny-mass lens (clustered roots are outside the
+    # linear regime of any finite difference): s=1, q=0.5, q3=0.3, r3=0.9, psi=1.1
+    e1 = 0.5 / 1.8
+    polys["10"] = np.asarray(ps._poly_coeffs_triple(w, 0.5, 0.9 * np.exp(1.1j), e1, 0.5 * e1))
+    for deg, c in polys.items():
+        lo = c[:, ::-1].copy()  # low -> high, as the primitive takes them
+        dp = (rng.normal(size=lo.shape) + 1j * rng.normal(size=lo.shape)) * np.abs(lo)
+        z = np.asarray(poly_roots(c, itmax=2500)).reshape(len(c), -1)
+        h = 1e-7
+        zp = np.asarray(poly_roots((lo + h * dp)[:, ::-1], itmax=2500)).reshape(len(c), -1)
+        zm = np.asarray(poly_roots((lo - h * dp)[:, ::-1], itmax=2500)).reshape(len(c), -1)
+        match = lambda zz: np.take_along_axis(zz, np.argmin(np.abs(zz[:, None, :] - z[:, :, None]), axis=2), axis=1)
+        out["p" + deg], out["dp" + deg], out["z" + deg] = lo, dp, z
+        out["dz" + deg] = (match(zp) - match(zm)) / (2 * h)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp)")
     args = ap.parse_args()
     lib, poly_roots = load_reference(args.ref)
     from caustics import point_source as ps
+    if args.only == "roots_jvp":
+        np.savez_compressed(os.path.join(HERE, "roots_jvp.npz"), **roots_jvp_fixture(poly_roots, ps))
+        return
     from caustics import extended_source as es
     from caustics import lightcurve as lc
     from caustics import multipole as mp
@@ -238,6 +269,7 @@ def main():
                                 q3=np.float64(q3), r3=np.float64(r3), psi=np.float64(psi), mag=mags)
     print(f"[golden] triple {time.time() - t0:.1f}s", flush=True)
 
+    out["roots_jvp"] = roots_jvp_fixture(poly_roots, ps)
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
     print(f"[golden] wrote {len(out)} fixtures in {time.time() - t0:.1f}s")

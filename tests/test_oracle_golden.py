@@ -194,3 +194,13 @@ def test_oracle_vs_reference_solver_random():
             lib.ref_ea_solve(300, deg, 2000, comp, 0, c.ctypes.data, init.ctypes.data, ref.ctypes.data)
             mine = O.ea_solve(c, itmax=2000, compensated=bool(comp), init_mode=1)
             assert np.max(np.abs(mine - ref) / np.maximum(np.abs(ref), 1)) < 1e-10
+
+
+def test_roots_jvp_kat(G):
+    """The primitive's implicit-function JVP (ehrlich_aberth_primitive.py:252-312)
+    against central differences of the reference solver's own roots."""
+    d = G("roots_jvp")
+    for deg, tol in (("5", 1e-7), ("10", 1e-5)):
+        dz = O.roots_jvp(d["p" + deg], d["z" + deg], d["dp" + deg])
+        ref = d["dz" + deg]
+        assert np.max(np.abs(dz - ref) / np.abs(ref)) < tol
