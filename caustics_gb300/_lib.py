@@ -64,6 +64,8 @@ SIGNATURES = {
                                                  ctypes.POINTER(EsOptions), _P, _P, _P]),
     "cgb_debug_record_len": (ctypes.c_int64, [ctypes.c_int32]),
     "cgb_mag_lc_batched_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+    "cgb_mag_lc_batched_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
+                                                  ctypes.POINTER(EsOptions), _P]),
     "cgb_mag_lc_batched": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
                                           ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
     "cgb_mag_lc_batched_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P,

@@ -357,4 +357,48 @@ int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho,
                      "cgb_mag contour pass launch");
 }
 
+// ---- batched light curves without any allocation ----
+// Some callers cannot hand over a workspace and must not allocate device memory
+// themselves: an XLA custom-call handler gets every buffer from XLA's own
+// buffer assignment (the reference's GPU kernel called cudaMalloc per call
+// instead, lib/ehrlich_aberth/kernels.cc.cu:72-76), and a plain C caller that
+// binds only this ABI may run where no allocator is at hand.  For them the
+// queue header and queue slots live in a fixed, file-scope device array.
+namespace {
+constexpr int64_t kNoAllocMaxPoints = 1 << 18;  // 262,144 light-curve points per call
+constexpr size_t kNoAllocScratchBytes = 16 + 8 * (size_t)kNoAllocMaxPoints;  // 2 MiB + 16 B per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+constexpr int kNoAllocMaxDevices = 64;
+void *g_noalloc_ptr[kNoAllocMaxDevices];  // device address of the scratch, per device ordinal
+std::mutex g_noalloc_mu;
+}  // namespace
+
+extern "C" int cgb_mag_lc_batched_noalloc(const int64_t *offsets, const double *t, const cgb_curve_params *curves,
+                                          int64_t ncurves, int64_t npoints, double *mag, uint8_t *route,
+                                          uint32_t *status, const cgb_es_options *opts, void *stream) {
+  if (npoints > kNoAllocMaxPoints)
+    return fail(CGB_ERR_UNSUPPORTED,
+                "cgb_mag_lc_batched_noalloc: npoints exceeds the static scratch (262144 points)%s");
+  int dev = -1;
+  int rc = cuda_status(cudaGetDevice(&dev), "cgb_mag_lc_batched_noalloc: current device");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(CGB_ERR_UNSUPPORTED, "cgb_mag_lc_batched_noalloc: device ordinal out of range%s");
+  void *ws = nullptr;
+  {
+    // first call on a device: resolve the array's address in that device's context
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      rc = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cgb_mag_lc_batched_noalloc: scratch address");
+      if (rc) return rc;
+      g_noalloc_ptr[dev] = p;
+    }
+    ws = g_noalloc_ptr[dev];
+  }
+  // the call zeroes the 16-byte queue header on `stream`; the slots need no reset
+  return cgb_mag_lc_batched(offsets, t, curves, ncurves, npoints, mag, route, status, opts, ws, kNoAllocScratchBytes,
+                            stream);
+}
+
 }  // extern "C"

@@ -156,6 +156,18 @@ int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_
                        int64_t npoints, double *mag, uint8_t *route, uint32_t *status, const cgb_es_options *opts,
                        void *workspace, size_t workspace_bytes, void *stream);
 
+/* cgb_mag_lc_batched without a workspace argument and without allocating: the
+ * queue lives in a file-scope device array of the library (2 MiB + 16 B per
+ * device), so npoints is limited to 262,144 (larger calls fail with
+ * CGB_ERR_UNSUPPORTED).  The first call on a device resolves the array's
+ * address in that device's context (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls on one device share the array: two
+ * calls in flight at the same time (other streams or threads) race on it and
+ * must be serialised by the caller.  No counterpart in the reference. */
+int cgb_mag_lc_batched_noalloc(const int64_t *offsets, const double *t, const cgb_curve_params *curves,
+                               int64_t ncurves, int64_t npoints, double *mag, uint8_t *route, uint32_t *status,
+                               const cgb_es_options *opts, void *stream);
+
 /* Vector-Jacobian product of cgb_mag_lc_batched: grad float64[ncurves, 8] =
  * sum over the curve's points of cot[i] * d mag_i / d(s, q, rho, u1, u0,
  * alpha, t0, tE).  Hand-written adjoint: implicit-function rule for the images,
