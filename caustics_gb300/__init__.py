@@ -6,6 +6,7 @@ signatures."""
 from .api import (  # noqa: F401
     BatchedLightCurves,
     LightCurveMagnification,
+    critical_and_caustic_curves,
     ehrlich_aberth,
     mag_extended_source_grad,
     mag_lc_batched,
@@ -22,4 +23,4 @@ from .api import (  # noqa: F401
 
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
            "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves",
-           "roots_jvp", "roots_vjp"]
+           "roots_jvp", "roots_vjp", "critical_and_caustic_curves"]

@@ -35,7 +35,8 @@ class LensParams(ctypes.Structure):
 class EsOptions(ctypes.Structure):
     _fields_ = [("npts_limb", ctypes.c_int32), ("limb_darkening", ctypes.c_int32), ("u1", ctypes.c_double),
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32)]
+                ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32),
+                ("grad_fp64_above", ctypes.c_double)]
 
 
 class CurveParams(ctypes.Structure):
@@ -50,6 +51,9 @@ SIGNATURES = {
     "cgb_gauss_legendre": (ctypes.c_int, [ctypes.c_int32, _P, _P]),
     "cgb_ea_solve": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "gpu_ehrlich_aberth": (None, [_P, _P, ctypes.c_char_p, ctypes.c_size_t]),
+    "cgb_critical_curves_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),
+    "cgb_critical_and_caustic_curves": (ctypes.c_int, [ctypes.c_int32, LensParams, ctypes.c_int32, _P, _P, _P, _P,
+                                                       ctypes.c_size_t, _P]),
     "cgb_ea_roots_jvp": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, _P]),
     "cgb_ea_roots_vjp": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P]),
     "cgb_mag_point_source": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, LensParams, ctypes.c_int32,

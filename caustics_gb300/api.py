@@ -6,6 +6,7 @@ Signature parity with fbartolic/caustics:
   mag_extended_source ........... src/caustics/extended_source.py:741-752
   mag ........................... src/caustics/lightcurve.py:99-110
   lens_eq, lens_eq_det_jac ...... src/caustics/point_source.py:1536-1580
+  critical_and_caustic_curves ... src/caustics/point_source.py:1582-1649
 
 Inputs may be torch tensors (any device; CUDA tensors stay on their device)
 or array-likes (copied to the current CUDA device; NumPy out).  Every
@@ -160,6 +161,38 @@ def poly_roots(coeffs, itmax=2000, compensated=False, custom_init=False, roots_i
 
 
 # ---------------------------------------------------------------------------
+# critical curves and caustics
+# ---------------------------------------------------------------------------
+
+def critical_and_caustic_curves(npts=200, nlenses=2, roots_itmax=2000, device=None, **params):
+    """(critical_curves, caustic_curves), each [2*nlenses, npts] complex, one
+    continuous curve per row, in the centre-of-mass frame
+    (point_source.py:1582-1649).  NumPy out, or CUDA tensors on `device`."""
+    dev = torch.device(device) if device is not None else None
+    if dev is None and not torch.cuda.is_available():
+        raise L.CausticsError("caustics_gb300 needs a CUDA device (no CPU fallback)")
+    dev = dev or torch.device("cuda", torch.cuda.current_device())
+    if nlenses == 1:  # the Einstein ring and a point caustic
+        phi = torch.linspace(-math.pi, math.pi, npts, dtype=torch.float64, device=dev)
+        zcr, zca = torch.exp(-1j * phi)[None, :], torch.zeros((1, npts), dtype=torch.complex128, device=dev)
+    else:
+        lens = L.lens_params(nlenses, params)
+        deg = 2 * nlenses
+        zcr = torch.empty((deg, npts), dtype=torch.complex128, device=dev)
+        zca = torch.empty((deg, npts), dtype=torch.complex128, device=dev)
+        nbytes = int(L.lib().cgb_critical_curves_workspace_bytes(npts, nlenses))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        with torch.cuda.device(dev):
+            L.check(L.lib().cgb_critical_and_caustic_curves(int(npts), lens, int(roots_itmax), _ptr(zcr), _ptr(zca),
+                                                            _ptr(st), _ptr(ws), nbytes, _stream()),
+                    "cgb_critical_and_caustic_curves")
+    if device is not None:
+        return zcr, zca
+    return zcr.cpu().numpy(), zca.cpu().numpy()
+
+
+# ---------------------------------------------------------------------------
 # lens equation helpers (elementwise, on device)
 # ---------------------------------------------------------------------------
 
@@ -238,9 +271,11 @@ def mag_point_source(w, nlenses=2, roots_itmax=2500, roots_compensated=False, pr
     return out[0] if len(out) == 1 else tuple(out)
 
 
-def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1):
+def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1,
+                grad_fp64_above=0.0):
     return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
-                       _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group))
+                       _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group),
+                       float(grad_fp64_above))
 
 
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
@@ -344,7 +379,7 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
 
 
 def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
-                       precision="mixed", grid=0, queue_chunk=1, ld_group=1):
+                       precision="mixed", grid=0, queue_chunk=1, ld_group=1, grad_fp64_above=0.0):
     """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c]."""
     off, tt, cv = _batched_args(offsets, t, curves)
     ct, _ = _to_device(cot, torch.float64)
@@ -354,7 +389,8 @@ def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=Fa
     route = torch.empty(n, dtype=torch.uint8, device=dev)
     grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
     ws, nbytes = _workspace(n, dev)
-    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group)
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
+                       grad_fp64_above)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched_vjp(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
                                                _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
@@ -370,7 +406,8 @@ class LightCurveMagnification(torch.autograd.Function):
     def forward(ctx, curves, offsets, t, options):
         ctx.save_for_backward(curves, offsets, t)
         ctx.options = dict(options)
-        return mag_lc_batched(offsets, t, curves.detach(), **ctx.options)
+        fwd = {k: v for k, v in ctx.options.items() if k != "grad_fp64_above"}
+        return mag_lc_batched(offsets, t, curves.detach(), **fwd)
 
     @staticmethod
     def backward(ctx, gmag):
@@ -380,9 +417,11 @@ class LightCurveMagnification(torch.autograd.Function):
 
 
 def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
-                             roots_itmax=2500, precision=None, grid=0, **params):
+                             roots_itmax=2500, precision=None, grid=0, grad_fp64_above=0.0, **params):
     """(mag [n], grad [n, 6]) with grad = d mag / d(s, q, rho, u1, Re w0, Im w0)
-    (binary lenses): the hand-written adjoint of mag_extended_source."""
+    (binary lenses): the hand-written adjoint of mag_extended_source.
+    grad_fp64_above: in "mixed", contour points whose image tangents exceed it
+    run the adjoint quadrature in FP64 (0 = default, < 0 = all)."""
     if nlenses != 2:
         raise ValueError("the adjoint supports binary lenses")
     wt, was_np = _to_device(np.atleast_1d(w0) if np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor) else w0,
@@ -391,7 +430,8 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
     n = wf.numel()
     mag_out = torch.empty(n, dtype=torch.float64, device=wf.device)
     g = torch.empty((n, 6), dtype=torch.float64, device=wf.device)
-    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid,
+                       grad_fp64_above=grad_fp64_above)
     with torch.cuda.device(wf.device):
         L.check(L.lib().cgb_mag_extended_source_grad(_ptr(wf), _ptr(mag_out), _ptr(g), n, float(rho),
                                                      L.lens_params(nlenses, params), opts, None, _stream()),

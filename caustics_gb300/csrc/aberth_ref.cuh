@@ -119,9 +119,9 @@ __device__ int solve(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm)
 
 // The same iteration spread over a group of G lanes (G a power of two >= DEG,
 // G <= 32; every lane of the group calls it together): lane r owns root r.
-// Root j's Horner values and stopping test depend on z_j alone, which nothing
-// changes before root j's own update, so all roots are evaluated at the start
-// of an iteration; then, for j in order, the terms 1/(z_j - z_i) are formed on
+// Root j's Horner values, stopping test and z_j^2 depend on z_j alone, which
+// nothing changes before root j's own update, so all roots are evaluated at the
+// start of an iteration; then, for j in order, the terms 1/(z_j - z_i) are formed on
 // lanes i and summed in the serial order, and lane j applies its correction.
 // The arithmetic of every value is that of solve(), so the iterates are the same
 // bit for bit, at about a quarter of the sequential FP64 instructions.
@@ -153,7 +153,7 @@ __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm)
   const double EPS = 1.1102230246251565e-16;
   for (int it = 0; it < itmax; ++it) {
     bool stop = false, rev = false;
-    cd h = cd{0.0, 0.0}, hd = cd{0.0, 0.0};
+    cd h = cd{0.0, 0.0}, hd = cd{0.0, 0.0}, zsq = cd{0.0, 0.0};
     if (r < DEG && !((conv >> r) & 1u)) {
       double az = absc(zr);
       rev = az > 1.0;
@@ -168,6 +168,7 @@ __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm)
         h = add(mul(h, x), rev ? p[k] : p[DEG - k]);
       }
       stop = !(absc(h) > __dmul_rn(EPS, b));
+      if (rev && !stop) zsq = sq_pow(zr);  // z_j^2 of the reversed correction, also from z_j alone
     }
     const uint32_t newly = (__ballot_sync(gmask, stop) >> (lane - r)) & all;
     for (int j = 0; j < DEG; ++j) {
@@ -184,7 +185,7 @@ __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm)
       if (r == j) {
         cd corr;
         if (rev) {
-          cd z2h = mul(sq_pow(zr), h);
+          cd z2h = mul(zsq, h);
           corr = div(z2h, sub(sub(scale(mul(zr, h), (double)DEG), hd), mul(z2h, s)));
         } else {
           corr = div(h, sub(hd, mul(h, s)));

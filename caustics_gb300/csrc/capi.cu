@@ -123,6 +123,13 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
   P.ld = o->limb_darkening ? 1 : 0;
   P.itmax = o->roots_itmax > 0 ? o->roots_itmax : 2500;
   P.ld_group = (o->ld_group == 2 || o->ld_group == 4 || o->ld_group == 8) ? o->ld_group : 1;
+  {
+    // default 2: on 64 random light curves x 1000 points the mixed VJP then
+    // matches the all-FP64 adjoint's agreement with finite differences, at
+    // 2.6x its speed (threshold 8: 4x faster, but 8e-4 from the FP64 gradient)
+    const double a = o->grad_fp64_above == 0.0 ? 2.0 : o->grad_fp64_above;
+    P.grad_amp2 = a < 0.0 ? -1.0 : a * a;
+  }
   P.qchunk = o->queue_chunk > 0 ? o->queue_chunk : 1;
   if (P.ld) {
     P.n1 = o->npts_ld / 2;
@@ -205,6 +212,26 @@ void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t
   memcpy(&d, opaque, sizeof(d));
   cgb_ea_solve((const double *)buffers[0], nullptr, (double *)buffers[1], d.size, d.deg, d.itmax,
                d.compensated ? CGB_PREC_FP64_COMP : CGB_PREC_FP64, nullptr, stream);
+}
+
+size_t cgb_critical_curves_workspace_bytes(int32_t npts, int32_t nlenses) {
+  return critical_workspace_bytes(npts, nlenses == 3 ? 3 : 2);
+}
+
+int cgb_critical_and_caustic_curves(int32_t npts, cgb_lens_params lens, int32_t itmax, double *z_cr, double *z_ca,
+                                    uint32_t *status, void *workspace, size_t workspace_bytes, void *stream) {
+  if (npts < 2 || npts > 16384) return fail(CGB_ERR_INVALID, "npts must be in [2, 16384]%s");
+  if (!lens_ok(lens)) return fail(CGB_ERR_INVALID, "invalid lens parameters%s");
+  if (itmax < 1) return fail(CGB_ERR_INVALID, "itmax must be >= 1%s");
+  if (!z_cr || !z_ca) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!workspace || workspace_bytes < critical_workspace_bytes(npts, lens.nlenses))
+    return fail(CGB_ERR_INVALID, "workspace too small (see cgb_critical_curves_workspace_bytes)%s");
+  if (status) {
+    int rc = cuda_status(cudaMemsetAsync(status, 0, sizeof(uint32_t), (cudaStream_t)stream), "status reset");
+    if (rc) return rc;
+  }
+  return cuda_status(launch_critical(lens_of(lens), npts, itmax, z_cr, z_ca, status, workspace, (cudaStream_t)stream),
+                     "cgb_critical_and_caustic_curves launch");
 }
 
 int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t *image_mask, int64_t n,

@@ -246,7 +246,7 @@ struct RefGroup {
 // call together (refea::solve_group); every lane returns the map.
 template <int NL>
 __device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, double th, const cd *zprev, uint64_t prev,
-                                       const cd *zcur, bool jitter) {
+                                       const cd *zcur, bool jitter, int &iters) {
   constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G;
   const int lane = threadIdx.x & 31, r = lane & (G - 1);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
@@ -259,7 +259,7 @@ __device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, doubl
     zr = zprev[perm_get(prev, r)];
     if (jitter) zr = zr + mk(1e-6 * ((r & 1) ? 0.5 : -0.5), 1e-6 * ((r & 2) ? 0.5 : -0.5));
   }
-  refea::solve_group<DEG, G>(p, zr, P.itmax, true);
+  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, true);
   cd z[DEG];
 #pragma unroll
   for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
@@ -270,7 +270,8 @@ __device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, doubl
 }
 
 template <int NL>
-__device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, double th, const cd *zraw) {
+__device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, double th, const cd *zraw,
+                                            int &iters) {
   constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G;
   const int lane = threadIdx.x & 31, r = lane & (G - 1);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
@@ -279,7 +280,7 @@ __device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, 
   cd p[DEG + 1];
   lens_poly<NL>(I.L, mk(__dadd_rn(__dmul_rn(I.rho, c), I.w0.x), __dadd_rn(__dmul_rn(I.rho, s), I.w0.y)), p);
   cd zr = mk(0.0, 0.0);
-  refea::solve_group<DEG, G>(p, zr, P.itmax, false);
+  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, false);
   cd z[DEG];
 #pragma unroll
   for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
@@ -865,24 +866,32 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
       const cd zc = S.Z[S.CP[i]], zp = S.Z[S.CP[ip]], zn = S.Z[S.CP[in]];
       if (P.ld) {
         const double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
-        PQGrad g;
-        if (PREC == MIXED)
-          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g);
-        else
-          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g);
-        const cd pq = S.PQ[i];
-        atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
-        atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
         // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2, so P_i wx_i + Q_i wy_i
         // contributes P_i (t_in - t_ip).x / 2 + Q_i (t_in - t_ip).y / 2 per
         // parameter.  Summed by parts against the FP64 image tangents rather than
         // scattered into the neighbours' position adjoints, where it would become
         // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
         // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
-        cd tn[6], tp[6];
+        cd tn[6], tp[6], ti[6];
         const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
         image_tangents(I, zn, S.TH[cpn / DEG], tn);
         image_tangents(I, zp, S.TH[cpp / DEG], tp);
+        image_tangents(I, zc, S.TH[S.CP[i] / DEG], ti);
+        // Near a critical curve the tangents grow like 1/|det J| and the
+        // pointwise contributions cancel in the sum; there the FP32 node values
+        // (relative error ~1e-7) would be amplified, so such points run the
+        // quadrature in FP64.
+        double amp2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
+        PQGrad g;
+        if (PREC == MIXED && amp2 <= P.grad_amp2)
+          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g);
+        else
+          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g);
+        const cd pq = mk(g.P, g.Q);
+        atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
+        atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
 #pragma unroll
         for (int k = 0; k < 6; ++k)
           acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
@@ -995,6 +1004,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   __shared__ uint32_t sflags;
   __shared__ int nsel_sh;
   __shared__ int nlist_sh;
+  __shared__ int dbg_ref[5];  // diagnostics: first-point iterations; A: solves, iterations; B: solves, iterations
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
   __shared__ EsItem item;
@@ -1104,7 +1114,10 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     uint32_t flags = 0;
     __syncthreads();
     const EsItem &I = item;
-    if (P.dbg && tid == 0) clk[0] = clock64();
+    if (P.dbg && tid == 0) {
+      clk[0] = clock64();
+      for (int c = 0; c < 5; ++c) dbg_ref[c] = 0;
+    }
 
     // ---- A: initial limb sampling (extended_source.py:100-107) ----
     const int n0 = P.n0;
@@ -1124,8 +1137,12 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     // and the chain is recomposed until no ambiguous map moves.
     constexpr int RG = RefGroup<DEG>::G;
     if (tid < RG) {
-      const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z);
-      if (tid == 0) S.PERM[0] = o;
+      int its;
+      const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z, its);
+      if (tid == 0) {
+        S.PERM[0] = o;
+        if (P.dbg) dbg_ref[0] += its;
+      }
     }
     for (int k = 1 + tid; k < n0; k += ES_THREADS) {
       bool amb;
@@ -1160,9 +1177,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       for (int e = tid / RG; e < nlist_sh; e += ES_THREADS / RG) {
         const int k = S.SCAN[e];
         const uint64_t prev = S.PERM[k - 1];
-        const uint64_t nb =
-            warm_map_ref_group<NL>(P, I, S.TH[k], S.Z + (size_t)(k - 1) * DEG, prev, S.Z + (size_t)k * DEG, false);
+        int its;
+        const uint64_t nb = warm_map_ref_group<NL>(P, I, S.TH[k], S.Z + (size_t)(k - 1) * DEG, prev,
+                                                   S.Z + (size_t)k * DEG, false, its);
         if ((tid & (RG - 1)) == 0) {
+          if (P.dbg) {
+            atomicAdd(&dbg_ref[1], 1);
+            atomicAdd(&dbg_ref[2], its);
+          }
           if (nb != S.BMAP[k]) {
             S.BMAP[k] = nb;
             nsel_sh = 1;
@@ -1240,9 +1262,16 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
         for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
         for (int e = tid / RG; e < nlist_sh; e += ES_THREADS / RG) {
           const int slot = (int)(S.USED[e] & 0xffffu), sl = (int)((S.USED[e] >> 16) & 0xffffu);
+          int its;
           const uint64_t m = warm_map_ref_group<NL>(P, I, S.TH[slot], S.Z + (size_t)sl * DEG, ident,
-                                                    S.Z + (size_t)slot * DEG, true);
-          if ((tid & (RG - 1)) == 0) apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+                                                    S.Z + (size_t)slot * DEG, true, its);
+          if ((tid & (RG - 1)) == 0) {
+            apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+            if (P.dbg) {
+              atomicAdd(&dbg_ref[3], 1);
+              atomicAdd(&dbg_ref[4], its);
+            }
+          }
         }
       }
       __syncthreads();
@@ -1530,6 +1559,9 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
         dbg[2] = S.M->flags;
         clk[6] = clock64();
         for (int c = 1; c < 7; ++c) dbg[ES_DBG_CLK + c - 1] = (double)(clk[c] - clk[c - 1]);
+        // faithful solves: A (chain repair) count + 1000 * first-point iterations; B count + 1000 * iterations
+        dbg[ES_DBG_CLK + 6] = dbg_ref[1] + 1000.0 * (dbg_ref[0] + dbg_ref[2]);
+        dbg[ES_DBG_CLK + 7] = dbg_ref[3] + 1000.0 * dbg_ref[4];
       }
       mag[pi] = fabs(tot) / (3.14159265358979323846 * I.rho * I.rho);
     }

@@ -18,6 +18,11 @@ cudaError_t launch_roots_jvp(const double *coeffs, const double *roots, const do
 cudaError_t launch_roots_vjp(const double *coeffs, const double *roots, const double *ct_roots, double *ct_coeffs,
                              int64_t n, int deg, int conjugate, cudaStream_t stream);
 
+// critical curves and caustics (critical.cu)
+size_t critical_workspace_bytes(int npts, int nlenses);
+cudaError_t launch_critical(const Lens &L, int npts, int itmax, double *z_cr, double *z_ca, uint32_t *status,
+                            void *ws, cudaStream_t stream);
+
 cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *images, uint32_t *image_mask,
                           int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream);
 

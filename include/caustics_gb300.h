@@ -61,6 +61,9 @@ typedef struct cgb_es_options {
   int32_t grid;           /* CTAs to launch, 0 = automatic */
   int32_t queue_chunk;    /* batched light curves: work items taken per queue grab (>= 1) */
   int32_t ld_group;       /* lanes sharing one contour point's quadrature nodes: 1, 2, 4 or 8 */
+  double grad_fp64_above; /* mixed-precision adjoints: a contour point whose image tangents |dz/dtheta|
+                             (own or neighbours', ~1/|det J|) exceed this runs its limb-darkening
+                             quadrature in FP64; 0 = default (2), < 0 = every point in FP64 */
 } cgb_es_options;
 
 /* Parameters of one binary-lens light curve for the batched entry points: lens
@@ -109,6 +112,18 @@ int cgb_ea_roots_vjp(const double *coeffs, const double *roots, const double *ct
  * (lib/ehrlich_aberth/kernels.h:11-20, gpu_ops.cc:14-25): buffers[0] = coeffs,
  * buffers[1] = roots.  Errors are reported through cgb_last_error(). */
 void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Critical curves and caustics of a binary or triple lens (replaces
+ * critical_and_caustic_curves, src/caustics/point_source.py:1582-1649): npts
+ * phases on linspace(-pi, pi, npts) (2 <= npts <= 16384), z_cr and z_ca
+ * complex128[2 * nlenses, npts], each row one continuous curve (greedy
+ * nearest chaining as the reference's match_points), both in the
+ * centre-of-mass frame.  status: optional uint32[1] (CGB_ST_NOCONV if a solve
+ * reached itmax; the reference's default itmax is 2000).  workspace: device
+ * bytes from cgb_critical_curves_workspace_bytes. */
+size_t cgb_critical_curves_workspace_bytes(int32_t npts, int32_t nlenses);
+int cgb_critical_and_caustic_curves(int32_t npts, cgb_lens_params lens, int32_t itmax, double *z_cr, double *z_ca,
+                                    uint32_t *status, void *workspace, size_t workspace_bytes, void *stream);
 
 /* Point-source magnification of n source positions w (complex128[n], in the
  * reference's centre-of-mass frame); mag: float64[n].  Optional outputs:
@@ -181,7 +196,9 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
 /* Diagnostics (no counterpart in the reference): cgb_mag_extended_source that
  * also writes, per point, a record of cgb_debug_record_len(npts_limb) doubles:
  * [L, n_contours, merge flags, (start, count, parity, integral) x 13,
- *  theta of the L limb points in limb order]. */
+ *  clock cycles of the six phases, faithful-labelling solves of the initial
+ *  chain (count + 1000 x iterations, first point included) and of the
+ *  refinement (same encoding), theta of the L limb points in limb order]. */
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                               const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
 int64_t cgb_debug_record_len(int32_t npts_limb);
