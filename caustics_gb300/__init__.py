@@ -5,6 +5,7 @@ behind a C ABI (include/caustics_gb300.h) with the reference's Python
 signatures."""
 from .api import (  # noqa: F401
     BatchedLightCurves,
+    LightCurveLogLikelihood,
     LightCurveMagnification,
     critical_and_caustic_curves,
     ehrlich_aberth,
@@ -16,6 +17,8 @@ from .api import (  # noqa: F401
     mag,
     mag_extended_source,
     mag_point_source,
+    marginalized_log_likelihood,
+    marginalized_log_likelihood_batched,
     poly_roots,
     roots_jvp,
     roots_vjp,
@@ -23,4 +26,5 @@ from .api import (  # noqa: F401
 
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
            "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves",
-           "roots_jvp", "roots_vjp", "critical_and_caustic_curves"]
+           "roots_jvp", "roots_vjp", "critical_and_caustic_curves",
+           "marginalized_log_likelihood", "marginalized_log_likelihood_batched", "LightCurveLogLikelihood"]

@@ -7,6 +7,7 @@ Signature parity with fbartolic/caustics:
   mag ........................... src/caustics/lightcurve.py:99-110
   lens_eq, lens_eq_det_jac ...... src/caustics/point_source.py:1536-1580
   critical_and_caustic_curves ... src/caustics/point_source.py:1582-1649
+  marginalized_log_likelihood ... src/caustics/linalg.py:10-94
 
 Inputs may be torch tensors (any device; CUDA tensors stay on their device)
 or array-likes (copied to the current CUDA device; NumPy out).  Every
@@ -437,6 +438,73 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
                                                      L.lens_params(nlenses, params), opts, None, _stream()),
                 "cgb_mag_extended_source_grad")
     return _out(mag_out, was_np), _out(g, was_np)
+
+
+# ---------------------------------------------------------------------------
+# marginalised likelihood
+# ---------------------------------------------------------------------------
+
+def marginalized_log_likelihood_batched(offsets, A, fobs, C_inv, ll_cot=None, return_grad=False):
+    """Per light curve c (points offsets[c] .. offsets[c+1]-1): (beta [n, 2],
+    ll [n]) and, with return_grad, d ll / d A (times ll_cot[c] if given)."""
+    off, _ = _to_device(offsets, torch.int64)
+    a, was_np = _to_device(A, torch.float64)
+    f, _ = _to_device(fobs, torch.float64)
+    c, _ = _to_device(C_inv, torch.float64)
+    n = off.numel() - 1
+    dev = a.device
+    beta = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    ll = torch.empty(n, dtype=torch.float64, device=dev)
+    g = torch.empty_like(a) if return_grad else None
+    lc = _to_device(ll_cot, torch.float64)[0] if ll_cot is not None else None
+    with torch.cuda.device(dev):
+        L.check(L.lib().cgb_marginalized_log_likelihood(_ptr(off), n, a.numel(), _ptr(a), _ptr(f), _ptr(c), _ptr(beta),
+                                                        _ptr(ll), _ptr(g), _ptr(lc), _stream()),
+                "cgb_marginalized_log_likelihood")
+    out = (_out(beta, was_np), _out(ll, was_np))
+    return out + (_out(g, was_np),) if return_grad else out
+
+
+def marginalized_log_likelihood(A_list, fobs_list, C_inv_list, dense_covariance=False, Lam_sd=1e04):
+    """(beta_list, ll): the log-likelihood summed over independent light curves,
+    marginalised over (F_s, F_b) (linalg.py:10-94, diagonal covariance)."""
+    if dense_covariance:
+        raise NotImplementedError("dense_covariance=True: the reference's dense branch does not run "
+                                  "(linalg.py:82-94 calls jnp.linals and an undefined M)")
+    parts = [(_to_device(a, torch.float64), _to_device(f, torch.float64)[0], _to_device(c, torch.float64)[0])
+             for a, f, c in zip(A_list, fobs_list, C_inv_list)]
+    was_np = all(p[0][1] for p in parts)
+    A = torch.cat([p[0][0].reshape(-1) for p in parts])
+    lens = [p[0][0].numel() for p in parts]
+    off = torch.as_tensor(np.concatenate([[0], np.cumsum(lens)]), dtype=torch.int64, device=A.device)
+    beta, ll = marginalized_log_likelihood_batched(off, A, torch.cat([p[1].reshape(-1) for p in parts]),
+                                                   torch.cat([p[2].reshape(-1) for p in parts]))
+    betas = [_out(b, was_np) for b in beta]
+    return betas, (float(ll.sum().item()) if was_np else ll.sum())
+
+
+class LightCurveLogLikelihood(torch.autograd.Function):
+    """Marginalised log-likelihood of batched light curves as a function of the
+    curve parameters: LightCurveLogLikelihood.apply(curves [n, 8], offsets, t,
+    fobs, C_inv, options) -> ll [n].  Backward: the likelihood's gradient with
+    respect to the magnifications is the cotangent of the light-curve VJP."""
+
+    @staticmethod
+    def forward(ctx, curves, offsets, t, fobs, C_inv, options):
+        ctx.options = dict(options)
+        fwd = {k: v for k, v in ctx.options.items() if k != "grad_fp64_above"}
+        mag = mag_lc_batched(offsets, t, curves.detach(), **fwd)
+        _, ll = marginalized_log_likelihood_batched(offsets, mag, fobs, C_inv)
+        ctx.save_for_backward(curves, offsets, t, fobs, C_inv, mag)
+        return ll
+
+    @staticmethod
+    def backward(ctx, gll):
+        curves, offsets, t, fobs, C_inv, mag = ctx.saved_tensors
+        _, _, cot = marginalized_log_likelihood_batched(offsets, mag, fobs, C_inv, ll_cot=gll.contiguous(),
+                                                        return_grad=True)
+        grad, _ = mag_lc_batched_vjp(offsets, t, curves.detach(), cot, **ctx.options)
+        return grad.to(curves.dtype), None, None, None, None, None
 
 
 class BatchedLightCurves:

@@ -130,8 +130,13 @@ __device__ __forceinline__ cd gshfl(unsigned mask, cd v, int src) {
   return cd{__shfl_sync(mask, v.x, src, G), __shfl_sync(mask, v.y, src, G)};
 }
 
+// With `target` (the DEG converged roots of the same polynomial, from a fast
+// solver) the iteration stops as soon as every iterate is clearly nearest one
+// of them (nearest distance below half the second nearest) and no two iterates
+// share a root: from there the iteration contracts each iterate onto that root,
+// so the labelling it produces is already decided.
 template <int DEG, int G>
-__device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm) {
+__device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm, const cd *target = nullptr) {
   static_assert(G >= DEG && G <= 32 && (G & (G - 1)) == 0, "group size");
   const int lane = threadIdx.x & 31, r = lane & (G - 1);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
@@ -195,6 +200,31 @@ __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm)
     }
     conv |= newly;
     if (conv == all) return it + 1;
+    if (target) {
+      bool clear = true;
+      uint32_t bit = 0;
+      if (r < DEG) {
+        double d1 = INFINITY, d2 = INFINITY;
+        int best = 0;
+#pragma unroll
+        for (int j = 0; j < DEG; ++j) {
+          const double d = norm2(target[j] - zr);
+          if (d < d1) {
+            d2 = d1;
+            d1 = d;
+            best = j;
+          } else if (d < d2) {
+            d2 = d;
+          }
+        }
+        clear = d1 < 0.25 * d2;
+        bit = 1u << best;
+      }
+#pragma unroll
+      for (int o = G >> 1; o > 0; o >>= 1) bit |= __shfl_xor_sync(gmask, bit, o, G);
+      const bool all_clear = __all_sync(gmask, clear);
+      if (all_clear && bit == all) return it + 1;
+    }
   }
   return -1;
 }

@@ -214,6 +214,16 @@ void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t
                d.compensated ? CGB_PREC_FP64_COMP : CGB_PREC_FP64, nullptr, stream);
 }
 
+int cgb_marginalized_log_likelihood(const int64_t *offsets, int64_t ncurves, int64_t npoints, const double *A,
+                                    const double *fobs, const double *C_inv, double *beta, double *ll,
+                                    double *dll_dA, const double *ll_cot, void *stream) {
+  if (ncurves < 0 || npoints < 0) return fail(CGB_ERR_INVALID, "ncurves and npoints must be >= 0%s");
+  if (ncurves == 0) return CGB_OK;
+  if (!offsets || !ll || (npoints > 0 && (!A || !fobs || !C_inv))) return fail(CGB_ERR_INVALID, "null buffer%s");
+  return cuda_status(launch_marg_ll(offsets, ncurves, A, fobs, C_inv, beta, ll, dll_dA, ll_cot, (cudaStream_t)stream),
+                     "cgb_marginalized_log_likelihood launch");
+}
+
 size_t cgb_critical_curves_workspace_bytes(int32_t npts, int32_t nlenses) {
   return critical_workspace_bytes(npts, nlenses == 3 ? 3 : 2);
 }

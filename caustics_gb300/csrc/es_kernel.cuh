@@ -259,7 +259,7 @@ __device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, doubl
     zr = zprev[perm_get(prev, r)];
     if (jitter) zr = zr + mk(1e-6 * ((r & 1) ? 0.5 : -0.5), 1e-6 * ((r & 2) ? 0.5 : -0.5));
   }
-  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, true);
+  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, true, zcur);
   cd z[DEG];
 #pragma unroll
   for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
@@ -280,7 +280,7 @@ __device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, 
   cd p[DEG + 1];
   lens_poly<NL>(I.L, mk(__dadd_rn(__dmul_rn(I.rho, c), I.w0.x), __dadd_rn(__dmul_rn(I.rho, s), I.w0.y)), p);
   cd zr = mk(0.0, 0.0);
-  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, false);
+  iters = refea::solve_group<DEG, G>(p, zr, P.itmax, false, zraw);
   cd z[DEG];
 #pragma unroll
   for (int t = 0; t < DEG; ++t) z[t] = refea::gshfl<G>(gmask, zr, t);
@@ -1327,6 +1327,53 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       }
     }
     __syncthreads();
+    // Change points of the open tracks (extended_source.py:156-216), found in
+    // parallel as bits per (track, position k = 0..L): START (a part starts at
+    // k), END (a part ends at k), NZ (a real, non-zero image at k).  The bits live
+    // in the candidate lists' storage, free after the chained matching.
+    const int W = (L + 1 + 63) >> 6;
+    uint64_t *bits = S.CAND;
+    const bool open_tracks = !S.M->all_closed;
+    if (open_tracks) {
+      for (int i = tid; i < 3 * DEG * W; i += ES_THREADS) bits[i] = 0ull;
+      __syncthreads();
+      for (int idx = tid; idx < DEG * (L + 1); idx += ES_THREADS) {
+        const int t = idx / (L + 1), k = idx - t * (L + 1);
+        auto real_at = [&](int kk) {
+          int slot = S.ORD[kk], row = perm_get(S.PERM[kk], t);
+          return (int)((S.MK[slot] >> row) & 1u);
+        };
+        auto par_at = [&](int kk) {
+          int slot = S.ORD[kk], row = perm_get(S.PERM[kk], t);
+          if (!((S.MK[slot] >> row) & 1u)) return 0;
+          if ((S.ZP[slot] >> row) & 1u) return 0;
+          return ((S.PP[slot] >> row) & 1u) ? 1 : -1;
+        };
+        int ch, dm;
+        if (k == 0) {
+          ch = real_at(0);
+          dm = real_at(0);
+        } else if (k == L) {
+          ch = real_at(L - 1);
+          dm = real_at(L - 1) ? -1 : 0;
+        } else {
+          int r0 = real_at(k - 1), r1 = real_at(k);
+          cd z0 = r0 ? V.at(t, k - 1) : mk(0, 0), z1 = r1 ? V.at(t, k) : mk(0, 0);
+          cd dz = z1 - z0;
+          bool jump = dz.x * dz.x + dz.y * dz.y > 0.1 * 0.1;
+          dm = r1 - r0;
+          ch = jump || (par_at(k) - par_at(k - 1) != 0) || (dm != 0);
+        }
+        const unsigned long long b = 1ull << (k & 63);
+        if (ch && dm >= 0) atomicOr((unsigned long long *)&bits[(0 * DEG + t) * W + (k >> 6)], b);
+        if (ch && dm <= 0) atomicOr((unsigned long long *)&bits[(1 * DEG + t) * W + (k >> 6)], b);
+        if (k < L && real_at(k)) {
+          const cd zz = V.at(t, k);
+          if (zz.x != 0.0 || zz.y != 0.0) atomicOr((unsigned long long *)&bits[(2 * DEG + t) * W + (k >> 6)], b);
+        }
+      }
+    }
+    __syncthreads();
     if (tid == 0) {
       MergeState &M = *S.M;
       // closed tracks in track order
@@ -1336,9 +1383,9 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           M.closed_tracks[j] = M.closed_tracks[j - 1];
           M.closed_tracks[j - 1] = x;
         }
-      if (!M.all_closed) {
-        // split open tracks (extended_source.py:156-216); parts ordered as
-        // argsort(nonempty)[::-1]: non-empty parts by descending (track, part)
+      if (open_tracks) {
+        // split open tracks; parts ordered as argsort(nonempty)[::-1]:
+        // non-empty parts by descending (track, part)
         int nseg_keep = 3 * DEG;
         int cand = 0;
         for (int t = DEG - 1; t >= 0; --t) {
@@ -1346,59 +1393,33 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           for (int i = 0; i < M.nclosed; ++i) closed |= M.closed_tracks[i] == t;
           int starts[10], ends[10], ns = 0, ne = 0;
           if (!closed) {
-            auto real_at = [&](int k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              return (int)((S.MK[slot] >> row) & 1u);
-            };
-            auto par_at = [&](int k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              if (!((S.MK[slot] >> row) & 1u)) return 0;
-              if ((S.ZP[slot] >> row) & 1u) return 0;
-              return ((S.PP[slot] >> row) & 1u) ? 1 : -1;
-            };
-            for (int k = 0; k <= L; ++k) {
-              int ch, dm;
-              if (k == 0) {
-                ch = real_at(0);
-                dm = real_at(0);
-              } else if (k == L) {
-                ch = real_at(L - 1);
-                dm = real_at(L - 1) ? -1 : 0;
-              } else {
-                int r0 = real_at(k - 1), r1 = real_at(k);
-                cd z0 = r0 ? V.at(t, k - 1) : mk(0, 0), z1 = r1 ? V.at(t, k) : mk(0, 0);
-                cd dz = z1 - z0;
-                bool jump = dz.x * dz.x + dz.y * dz.y > 0.1 * 0.1;
-                dm = r1 - r0;
-                ch = jump || (par_at(k) - par_at(k - 1) != 0) || (dm != 0);
-              }
-              if (ch && dm >= 0 && ns < 10) starts[ns++] = k;
-              if (ch && dm <= 0 && ne < 10) ends[ne++] = k;
-            }
+            for (int w = 0; w < W && ns < 10; ++w)
+              for (uint64_t x = bits[(0 * DEG + t) * W + w]; x && ns < 10; x &= x - 1)
+                starts[ns++] = (w << 6) + __ffsll((long long)x) - 1;
+            for (int w = 0; w < W && ne < 10; ++w)
+              for (uint64_t x = bits[(1 * DEG + t) * W + w]; x && ne < 10; x &= x - 1)
+                ends[ne++] = (w << 6) + __ffsll((long long)x) - 1;
           }
           for (int q = 9; q >= 0; --q) {
             int l = q < ns ? starts[q] : 0, r = q < ne ? ends[q] : 0;
             if (l == 0 && r == 0) continue;
-            int cnt = 0;
-            for (int k = l; k < r; ++k) {
-              int slot = S.ORD[k], row = perm_get(S.PERM[k], t);
-              if ((S.MK[slot] >> row) & 1u) {
-                cd zz = S.Z[(size_t)slot * DEG + row];
-                cnt += (zz.x != 0.0 || zz.y != 0.0);
-              }
+            int cnt = 0;  // real, non-zero images in [l, r)
+            for (int w = l >> 6; l < r && w <= ((r - 1) >> 6); ++w) {
+              uint64_t x = bits[(2 * DEG + t) * W + w];
+              if (w == (l >> 6)) x &= ~0ull << (l & 63);
+              if (w == ((r - 1) >> 6) && ((r - 1) & 63) != 63) x &= (2ull << ((r - 1) & 63)) - 1ull;
+              cnt += __popcll(x);
             }
             if (cnt < 2) continue;
             if (cand < nseg_keep) {
-              Segment &s = M.seg[cand];
-              s.t = (int16_t)t;
-              s.l = (int16_t)l;
-              s.r = (int16_t)r;
+              Segment &sg = M.seg[cand];
+              sg.t = (int16_t)t;
+              sg.l = (int16_t)l;
+              sg.r = (int16_t)r;
               int slot = S.ORD[l], row = perm_get(S.PERM[l], t);
-              s.par = ((S.ZP[slot] >> row) & 1u) ? 0 : (((S.PP[slot] >> row) & 1u) ? 1 : -1);
-              s.alive = 1;
-              double len = 0.0;
-              for (int k = l; k + 1 < r; ++k) len += cabs(V.at(t, k + 1) - V.at(t, k));
-              s.len = len;
+              sg.par = ((S.ZP[slot] >> row) & 1u) ? 0 : (((S.PP[slot] >> row) & 1u) ? 1 : -1);
+              sg.alive = 1;
+              sg.len = 0.0;
             }
             ++cand;
           }
@@ -1409,8 +1430,22 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           M.seg[i] = Segment{0, 0, 0, 0, 0.0, 0};
         }
         M.nseg = nseg_keep;
-        merge_segments<DEG>(S, L);
       }
+    }
+    __syncthreads();
+    if (open_tracks) {
+      // path length of every segment: one warp each
+      for (int q = warp; q < S.M->nseg; q += ES_WARPS) {
+        const Segment sg = S.M->seg[q];
+        if (!sg.alive) continue;
+        double len = 0.0;
+        for (int k = sg.l + lane; k + 1 < sg.r; k += 32) len += cabs(V.at(sg.t, k + 1) - V.at(sg.t, k));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) len += __shfl_xor_sync(0xffffffffu, len, o);
+        if (lane == 0) S.M->seg[q].len = len;
+      }
+      __syncthreads();
+      if (tid == 0) merge_segments<DEG>(S, L);
     }
     __syncthreads();
     if (P.dbg && tid == 0) clk[4] = clock64();

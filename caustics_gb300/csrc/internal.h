@@ -18,6 +18,11 @@ cudaError_t launch_roots_jvp(const double *coeffs, const double *roots, const do
 cudaError_t launch_roots_vjp(const double *coeffs, const double *roots, const double *ct_roots, double *ct_coeffs,
                              int64_t n, int deg, int conjugate, cudaStream_t stream);
 
+// marginalised log-likelihood over (F_s, F_b), diagonal covariance (likelihood.cu)
+cudaError_t launch_marg_ll(const int64_t *offsets, int64_t ncurves, const double *A, const double *fobs,
+                           const double *C_inv, double *beta, double *ll, double *dll, const double *ll_cot,
+                           cudaStream_t stream);
+
 // critical curves and caustics (critical.cu)
 size_t critical_workspace_bytes(int npts, int nlenses);
 cudaError_t launch_critical(const Lens &L, int npts, int itmax, double *z_cr, double *z_ca, uint32_t *status,

@@ -113,6 +113,21 @@ int cgb_ea_roots_vjp(const double *coeffs, const double *roots, const double *ct
  * buffers[1] = roots.  Errors are reported through cgb_last_error(). */
 void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* Log-likelihood of ncurves light curves marginalised over the linear flux
+ * parameters (F_s, F_b) with a diagonal inverse covariance (replaces
+ * marginalized_log_likelihood(..., dense_covariance=False),
+ * src/caustics/linalg.py:10-94; its dense branch does not run in the
+ * reference and has no counterpart).  Points offsets[c] .. offsets[c+1]-1
+ * (int64, device) of A (magnifications), fobs and C_inv (float64[npoints])
+ * belong to curve c.  Outputs: ll float64[ncurves] (the reference returns their
+ * sum), optional beta float64[ncurves, 2] = (F_s, F_b), optional dll_dA
+ * float64[npoints] = ll_cot[c] * d ll_c / d A_i (ll_cot optional, 1 if null),
+ * the cotangent that cgb_mag_lc_batched_vjp takes.  Curves whose normal matrix
+ * is singular (fewer than two distinct magnifications) give NaN. */
+int cgb_marginalized_log_likelihood(const int64_t *offsets, int64_t ncurves, int64_t npoints, const double *A,
+                                    const double *fobs, const double *C_inv, double *beta, double *ll,
+                                    double *dll_dA, const double *ll_cot, void *stream);
+
 /* Critical curves and caustics of a binary or triple lens (replaces
  * critical_and_caustic_curves, src/caustics/point_source.py:1582-1649): npts
  * phases on linspace(-pi, pi, npts) (2 <= npts <= 16384), z_cr and z_ca

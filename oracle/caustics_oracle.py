@@ -871,3 +871,34 @@ def frozen_gradient(w, rho, s, q, npts_limb, limb_darkening=False, u1=0.0, npts_
             vals.append(mag_es_frozen(st, p["w"], p["rho"], p["s"], p["q"], limb_darkening, p["u1"], npts_ld))
         g[k] = (vals[0] - vals[1]) / (2 * h)
     return g
+
+
+# ----------------------------------------------------------------------------
+# Marginalised likelihood (linalg.py:10-94, diagonal covariance branch)
+# ----------------------------------------------------------------------------
+
+
+def marginalized_log_likelihood(A_list, fobs_list, C_inv_list):
+    """Per light curve: weighted least squares for beta = (F_s, F_b) in
+    f = F_s A + F_b (linalg.py:60-66), then
+    ll = -chi2/2 + log det(2 pi Sigma)/2 with Sigma = (M^T C^-1 M)^-1 (:69-70).
+    Returns (beta [n, 2], ll per curve); the reference returns the sum."""
+    betas, lls = [], []
+    for A, f, c in zip(A_list, fobs_list, C_inv_list):
+        A, f, c = (np.asarray(x, dtype=np.float64) for x in (A, f, c))
+        M = np.stack([A, np.ones_like(A)], axis=1)
+        F = M.T @ (c[:, None] * M)
+        Sig = np.linalg.inv(F)
+        beta = Sig @ (M.T @ (c * f))
+        r = f - M @ beta
+        betas.append(beta)
+        lls.append(-0.5 * np.sum(r * r * c) + 0.5 * np.log(np.linalg.det(2 * np.pi * Sig)))
+    return np.array(betas), np.array(lls)
+
+
+def marginalized_log_likelihood_grad(A, fobs, C_inv, beta, Sigma):
+    """d ll / d A_i of one curve.  beta is the least-squares optimum, so chi2's
+    dependence through beta drops out (envelope theorem):
+    d ll / d A_i = c_i (r_i beta_0 - A_i Sigma_00 - Sigma_01)."""
+    r = fobs - (beta[0] * A + beta[1])
+    return C_inv * (r * beta[0] - A * Sigma[0, 0] - Sigma[0, 1])

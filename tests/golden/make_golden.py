@@ -17,7 +17,7 @@ Known deviations of this harness from the reference under real JAX:
 * roots come from the reference's C++ solver through ctypes instead of an XLA
   custom call (identical code, compiled with g++ -O2 -DNDEBUG).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp]
+Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp|likelihood]
 """
 import argparse
 import ctypes
@@ -125,15 +125,37 @@ def roots_jvp_fixture(poly_roots, ps):
     return out
 
 
+def likelihood_fixture():
+    """marginalized_log_likelihood (linalg.py:10-94, diagonal covariance) on
+    three light curves of uneven length: the list total and each curve alone."""
+    from caustics import linalg as la
+    rng = np.random.default_rng(31)
+    lens = [150, 400, 37]
+    A, f, c = [], [], []
+    for n, (fs, fb, sig) in zip(lens, [(2.0, 0.5, 0.05), (0.7, 1.3, 0.02), (5.0, -0.2, 0.3)]):
+        a = 1.0 + 3.0 * np.abs(rng.normal(size=n))
+        A.append(a)
+        f.append(fs * a + fb + sig * rng.normal(size=n))
+        c.append(np.full(n, 1.0 / sig ** 2) * rng.uniform(0.5, 1.5, n))
+    beta, ll = la.marginalized_log_likelihood(A, f, c)
+    ll_each = np.array([float(la.marginalized_log_likelihood([a], [ff], [cc])[1]) for a, ff, cc in zip(A, f, c)])
+    return dict(offsets=np.concatenate([[0], np.cumsum(lens)]).astype(np.int64), A=np.concatenate(A),
+                fobs=np.concatenate(f), C_inv=np.concatenate(c), beta=np.stack([np.asarray(b) for b in beta]),
+                ll=np.float64(ll), ll_each=ll_each)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp)")
+    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp, likelihood)")
     args = ap.parse_args()
     lib, poly_roots = load_reference(args.ref)
     from caustics import point_source as ps
     if args.only == "roots_jvp":
         np.savez_compressed(os.path.join(HERE, "roots_jvp.npz"), **roots_jvp_fixture(poly_roots, ps))
+        return
+    if args.only == "likelihood":
+        np.savez_compressed(os.path.join(HERE, "likelihood.npz"), **likelihood_fixture())
         return
     from caustics import extended_source as es
     from caustics import lightcurve as lc
@@ -270,6 +292,7 @@ def main():
     print(f"[golden] triple {time.time() - t0:.1f}s", flush=True)
 
     out["roots_jvp"] = roots_jvp_fixture(poly_roots, ps)
+    out["likelihood"] = likelihood_fixture()
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
     print(f"[golden] wrote {len(out)} fixtures in {time.time() - t0:.1f}s")

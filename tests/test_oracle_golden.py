@@ -204,3 +204,33 @@ def test_roots_jvp_kat(G):
         dz = O.roots_jvp(d["p" + deg], d["z" + deg], d["dp" + deg])
         ref = d["dz" + deg]
         assert np.max(np.abs(dz - ref) / np.abs(ref)) < tol
+
+
+def test_likelihood_kat(G):
+    """marginalized_log_likelihood (linalg.py:10-94, diagonal covariance) on the
+    reference's own output: per-curve beta and ll, and the list total."""
+    d = G("likelihood")
+    off = d["offsets"]
+    sl = [slice(off[i], off[i + 1]) for i in range(len(off) - 1)]
+    beta, ll = O.marginalized_log_likelihood([d["A"][s] for s in sl], [d["fobs"][s] for s in sl],
+                                             [d["C_inv"][s] for s in sl])
+    assert np.max(np.abs(beta - d["beta"]) / np.abs(d["beta"])) < 1e-11
+    assert np.max(np.abs(ll - d["ll_each"]) / np.abs(d["ll_each"])) < 1e-13
+    assert abs(ll.sum() - d["ll"]) < 1e-13 * abs(d["ll"])
+
+
+def test_likelihood_gradient_restatement(G):
+    """The closed-form d ll / d A against central differences of the oracle."""
+    d = G("likelihood")
+    a, f, c = d["A"][:150], d["fobs"][:150], d["C_inv"][:150]
+    M = np.stack([a, np.ones_like(a)], axis=1)
+    Sig = np.linalg.inv(M.T @ (c[:, None] * M))
+    beta, _ = O.marginalized_log_likelihood([a], [f], [c])
+    g = O.marginalized_log_likelihood_grad(a, f, c, beta[0], Sig)
+    for i in (0, 17, 149):
+        h = 1e-6 * a[i]
+        ap, am = a.copy(), a.copy()
+        ap[i] += h
+        am[i] -= h
+        fd = (O.marginalized_log_likelihood([ap], [f], [c])[1][0] - O.marginalized_log_likelihood([am], [f], [c])[1][0]) / (2 * h)
+        assert abs(fd - g[i]) < 1e-6 * max(abs(g[i]), 1.0)
