@@ -36,7 +36,7 @@ class EsOptions(ctypes.Structure):
     _fields_ = [("npts_limb", ctypes.c_int32), ("limb_darkening", ctypes.c_int32), ("u1", ctypes.c_double),
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32),
-                ("grad_fp64_above", ctypes.c_double)]
+                ("labelling", ctypes.c_int32), ("grad_fp64_above", ctypes.c_double)]
 
 
 class CurveParams(ctypes.Structure):

@@ -272,18 +272,25 @@ def mag_point_source(w, nlenses=2, roots_itmax=2500, roots_compensated=False, pr
     return out[0] if len(out) == 1 else tuple(out)
 
 
+_LABELLING = {"reference": 0, "nearest": 1}
+
+
 def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1,
-                grad_fp64_above=0.0):
+                grad_fp64_above=0.0, labelling="reference"):
+    if labelling not in _LABELLING:
+        raise ValueError(f"labelling must be one of {sorted(_LABELLING)}")
     return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
                        _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group),
-                       float(grad_fp64_above))
+                       _LABELLING[labelling], float(grad_fp64_above))
 
 
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
                         roots_itmax=2500, roots_compensated=False, precision=None, return_status=False, grid=0,
-                        **params):
+                        labelling="reference", **params):
     """Extended-source magnification (extended_source.py:741-904).  w0 may be a
-    scalar (as in the reference) or an array of source centres (batched)."""
+    scalar (as in the reference) or an array of source centres (batched).
+    labelling: "reference" reproduces the reference's limb image row order
+    exactly; "nearest" matches roots by distance everywhere (faster)."""
     scalar = np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor)
     wt, was_np = _to_device(np.atleast_1d(w0) if scalar else w0, torch.complex128)
     shape = wt.shape
@@ -291,7 +298,7 @@ def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False,
     n = wf.numel()
     mag = torch.empty(n, dtype=torch.float64, device=wf.device)
     st = torch.zeros(n, dtype=torch.int32, device=wf.device)
-    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling)
     with torch.cuda.device(wf.device):
         L.check(L.lib().cgb_mag_extended_source(_ptr(wf), _ptr(mag), n, float(rho), L.lens_params(nlenses, params),
                                                 opts, _ptr(st), _stream()), "cgb_mag_extended_source")
@@ -303,7 +310,8 @@ def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False,
 
 
 def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, npts_ld=100, roots_itmax=2500,
-        roots_compensated=False, precision=None, return_route=False, return_status=False, grid=0, **params):
+        roots_compensated=False, precision=None, return_route=False, return_status=False, grid=0,
+        labelling="reference", **params):
     """Light curve: hexadecapole where the reference's tests accept it, contour
     integration elsewhere (lightcurve.py:99-254)."""
     wt, was_np = _to_device(w_points, torch.complex128)
@@ -313,7 +321,7 @@ def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, n
     out = torch.empty(n, dtype=torch.float64, device=wf.device)
     route = torch.empty(n, dtype=torch.uint8, device=wf.device)
     st = torch.zeros(n, dtype=torch.int32, device=wf.device)
-    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling)
     with torch.cuda.device(wf.device):
         L.check(L.lib().cgb_mag(_ptr(wf), _ptr(out), _ptr(route), n, float(rho), L.lens_params(nlenses, params), opts,
                                 _ptr(st), _stream()), "cgb_mag")
@@ -350,7 +358,7 @@ def _workspace(n, device):
 
 def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
                    precision="mixed", grid=0, queue_chunk=1, ld_group=1, return_route=False, return_status=False,
-                   out=None):
+                   out=None, labelling="reference"):
     """mag() for many binary-lens light curves of uneven lengths in one pass.
 
     offsets: int64 [ncurves+1]; t: float64 [npoints]; curves: float64
@@ -367,7 +375,8 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
     else:  # caller-owned buffers (fixed-shape / graph-captured use)
         mag_out, route, st, ws = out
         nbytes = ws.numel()
-    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group)
+    opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
+                       labelling=labelling)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
                                            _ptr(st), opts, _ptr(ws), nbytes, _stream()), "cgb_mag_lc_batched")
@@ -380,7 +389,8 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
 
 
 def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
-                       precision="mixed", grid=0, queue_chunk=1, ld_group=1, grad_fp64_above=0.0):
+                       precision="mixed", grid=0, queue_chunk=1, ld_group=1, grad_fp64_above=0.0,
+                       labelling="reference"):
     """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c]."""
     off, tt, cv = _batched_args(offsets, t, curves)
     ct, _ = _to_device(cot, torch.float64)
@@ -391,7 +401,7 @@ def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=Fa
     grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
     ws, nbytes = _workspace(n, dev)
     opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
-                       grad_fp64_above)
+                       grad_fp64_above, labelling)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched_vjp(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
                                                _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
@@ -418,7 +428,8 @@ class LightCurveMagnification(torch.autograd.Function):
 
 
 def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
-                             roots_itmax=2500, precision=None, grid=0, grad_fp64_above=0.0, **params):
+                             roots_itmax=2500, precision=None, grid=0, grad_fp64_above=0.0, labelling="reference",
+                             **params):
     """(mag [n], grad [n, 6]) with grad = d mag / d(s, q, rho, u1, Re w0, Im w0)
     (binary lenses): the hand-written adjoint of mag_extended_source.
     grad_fp64_above: in "mixed", contour points whose image tangents exceed it
@@ -432,7 +443,7 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
     mag_out = torch.empty(n, dtype=torch.float64, device=wf.device)
     g = torch.empty((n, 6), dtype=torch.float64, device=wf.device)
     opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid,
-                       grad_fp64_above=grad_fp64_above)
+                       grad_fp64_above=grad_fp64_above, labelling=labelling)
     with torch.cuda.device(wf.device):
         L.check(L.lib().cgb_mag_extended_source_grad(_ptr(wf), _ptr(mag_out), _ptr(g), n, float(rho),
                                                      L.lens_params(nlenses, params), opts, None, _stream()),

@@ -1136,7 +1136,13 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     // reference's warm start from the predecessor in the current chain order,
     // and the chain is recomposed until no ambiguous map moves.
     constexpr int RG = RefGroup<DEG>::G;
-    if (tid < RG) {
+    if (P.nearest) {
+      if (tid == 0) {
+        uint64_t ident = 0;
+        for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
+        S.PERM[0] = ident;
+      }
+    } else if (tid < RG) {
       int its;
       const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z, its);
       if (tid == 0) {
@@ -1147,7 +1153,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     for (int k = 1 + tid; k < n0; k += ES_THREADS) {
       bool amb;
       S.BMAP[k] = step_map<DEG>(S.Z + (size_t)(k - 1) * DEG, S.Z + (size_t)k * DEG, amb);
-      S.USED[k] = amb ? ~0ull : 0ull;  // 0: clear step, map final
+      S.USED[k] = (amb && !P.nearest) ? ~0ull : 0ull;  // 0: map final (clear step, or nearest labelling)
     }
     __syncthreads();
     for (int round = 0; round < 12; ++round) {
@@ -1250,7 +1256,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
                                      S.PP[slot], S.ZP[slot], flags);
           bool amb;
           const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
-          if (amb)  // labelled below by the reference's warm start, on a lane group
+          if (amb && !P.nearest)  // labelled below by the reference's warm start, on a lane group
             S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
           else
             apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);

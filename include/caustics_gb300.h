@@ -61,6 +61,10 @@ typedef struct cgb_es_options {
   int32_t grid;           /* CTAs to launch, 0 = automatic */
   int32_t queue_chunk;    /* batched light curves: work items taken per queue grab (>= 1) */
   int32_t ld_group;       /* lanes sharing one contour point's quadrature nodes: 1, 2, 4 or 8 */
+  int32_t labelling;      /* limb image row order: 0 = the reference's warm-start chain, reproduced
+                             exactly (faithful FP64 solves on ambiguous steps); 1 = nearest-root
+                             matching everywhere (faster; the result moves within the reference's own
+                             sensitivity to its warm-start jitter, ~3e-5) */
   double grad_fp64_above; /* mixed-precision adjoints: a contour point whose image tangents |dz/dtheta|
                              (own or neighbours', ~1/|det J|) exceed this runs its limb-darkening
                              quadrature in FP64; 0 = default (2), < 0 = every point in FP64 */

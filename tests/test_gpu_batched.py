@@ -115,7 +115,9 @@ def test_autograd_function_backward_is_the_vjp():
     cot = torch.randn_like(m)
     (m * cot).sum().backward()
     g, _ = C.mag_lc_batched_vjp(offs, tt, curves.detach(), cot, **opts)
-    assert torch.allclose(curves.grad, g, rtol=1e-12, atol=0)
+    # per-curve sums are accumulated with atomics, so two identical calls agree
+    # only up to the summation order of point contributions
+    assert torch.allclose(curves.grad, g, rtol=1e-9, atol=1e-12 * float(g.abs().max()))
 
 
 def test_autotuned_graph_evaluator():
