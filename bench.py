@@ -458,6 +458,13 @@ def main():
         fp64_peak = fma_peak(1)
         es64_ms = timed(stream, lambda: C.mag_extended_source(w, WL["rho"], precision="fp64", **kw), flush=flush)
 
+        # nearest-root labelling: no faithful labelling solves
+        near = C.BatchedLightCurves(offsets, t_dev, curves_for_tuning=curves, precision="mixed", labelling="nearest",
+                                    config=ev.config, **kwb)
+        near(curves)
+        near_ms = timed(stream, lambda: near(curves), reps=max(2, args.steps), flush=flush)
+        near_err = float(torch.max(torch.abs(near.mag - out64) / out64).item())
+
         # VJP of the light curve (s, q, rho, u1, u0, alpha, t0, tE) with a N(0,1) cotangent
         C.mag_lc_batched_vjp(offsets, t_dev, curves, cot, precision="mixed", **ev.config, **kwb)
         vjp_ms = timed(stream, lambda: C.mag_lc_batched_vjp(offsets, t_dev, curves, cot, precision="mixed",
@@ -482,6 +489,8 @@ def main():
             "batched_mixed_vs_plain_fp64": value / world / plain_rate,
             "mixed_vs_fp64_max_rel_err": err,
             "vjp_evals_per_s": vjp_rate,
+            "nearest_labelling": {"evals_per_s": WL["npoints"] / (near_ms * 1e-3),
+                                  "max_rel_err_vs_fp64_reference_labelling": near_err},
             "vjp_plus_forward_vs_plain_fp64": 1.0 / ((1.0 / value * world + 1.0 / vjp_rate) * plain_rate),
             "fp64_roofline": {"kernel": "es_kernel<2,FP64>", "achieved": WL["npoints"] * FLOP_PER_EVAL /
                               (es64_ms * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",

@@ -526,7 +526,7 @@ class BatchedLightCurves:
     curve parameters; the launch shape comes from the autotuner."""
 
     def __init__(self, offsets, t, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
-                 precision="mixed", tune=True, graph=True, curves_for_tuning=None, config=None):
+                 precision="mixed", tune=True, graph=True, curves_for_tuning=None, config=None, labelling="reference"):
         from . import autotune
         self.offsets, _ = _to_device(offsets, torch.int64)
         self.t, _ = _to_device(t, torch.float64)
@@ -538,7 +538,7 @@ class BatchedLightCurves:
         self.status = torch.zeros(n, dtype=torch.int32, device=dev)
         self.ws, _ = _workspace(n, dev)
         self.kw = dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=roots_itmax,
-                       precision=precision)
+                       precision=precision, labelling=labelling)
         if config is None:
             config = (autotune.tune(self.offsets, self.t, curves_for_tuning, **self.kw)
                       if tune and curves_for_tuning is not None else autotune.DEFAULT)

@@ -24,19 +24,20 @@ def _sample(offsets, t, curves, max_points):
 
 
 def tune(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500, precision="mixed",
-         max_points=4096, reps=2, verbose=False):
+         max_points=4096, reps=2, verbose=False, labelling="reference"):
     from . import api
     offsets, _ = api._to_device(offsets, torch.int64)
     t, _ = api._to_device(t, torch.float64)
     curves, _ = api._to_device(curves, torch.float64)
     dev = t.device
-    key = (torch.cuda.get_device_name(dev), int(npts_limb), bool(limb_darkening), int(npts_ld), str(precision))
+    key = (torch.cuda.get_device_name(dev), int(npts_limb), bool(limb_darkening), int(npts_ld), str(precision),
+           str(labelling))
     if key in _CACHE:
         return dict(_CACHE[key])
     so, st, sc = _sample(offsets, t, curves, max_points)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     kw = dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=roots_itmax,
-              precision=precision)
+              precision=precision, labelling=labelling)
     best, best_ms, table = None, float("inf"), []
     for per_sm, chunk, group in itertools.product((1, 2), (1, 2, 4), (1, 2, 4)):
         cfg = dict(grid=per_sm * sms, queue_chunk=chunk, ld_group=group)
