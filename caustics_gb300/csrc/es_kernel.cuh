@@ -189,10 +189,10 @@ __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, 
 #pragma unroll
   for (int i = 0; i < DEG; ++i) {
     zrow[i] = z[i];
-    double r = cabs(lens_eq<NL>(I.L, z[i]) - w);
+    const double r = cabs(lens_eq<NL>(I.L, z[i]) - w);
+    const double d = lens_det<NL>(I.L, z[i]);
     if (r < 1e-6) mkb |= 1u << i;
     if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
-    double d = lens_det<NL>(I.L, z[i]);
     if (d > 0) pp |= 1u << i;
     if (d == 0) zp |= 1u << i;
   }
@@ -1005,6 +1005,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   __shared__ int nsel_sh;
   __shared__ int nlist_sh;
   __shared__ int dbg_ref[5];  // diagnostics: first-point iterations; A: solves, iterations; B: solves, iterations
+  __shared__ long long dbg_b[4];  // diagnostics: refinement clocks (gaps+rank+scan, solves, labelling, insertion)
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
   __shared__ EsItem item;
@@ -1117,6 +1118,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     if (P.dbg && tid == 0) {
       clk[0] = clock64();
       for (int c = 0; c < 5; ++c) dbg_ref[c] = 0;
+      for (int c = 0; c < 4; ++c) dbg_b[c] = 0;
     }
 
     // ---- A: initial limb sampling (extended_source.py:100-107) ----
@@ -1210,7 +1212,9 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
 
     // ---- B: refinement rounds (extended_source.py:109-135) ----
     int Lcur = n0;
+    long long tb = 0;
     for (int round = 0; round < P.niter; ++round) {
+      if (P.dbg && tid == 0) tb = clock64();
       const int ngap = Lcur - 1;
       for (int k = tid; k < ngap; k += ES_THREADS) {
         const int s1 = S.ORD[k], s2 = S.ORD[k + 1];
@@ -1242,6 +1246,11 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
       __syncthreads();
       int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);
+      if (P.dbg && tid == 0) {
+        const long long t = clock64();
+        dbg_b[0] += t - tb;
+        tb = t;
+      }
       // new slots: selected gap k -> slot Lcur + SCAN[k]
       for (int k = tid; k < ngap; k += ES_THREADS) {
         if (S.KEY[k] != 0.0) {
@@ -1263,6 +1272,11 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
         }
       }
       __syncthreads();
+      if (P.dbg && tid == 0) {
+        const long long t = clock64();
+        dbg_b[1] += t - tb;
+        tb = t;
+      }
       {
         uint64_t ident = 0;
         for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
@@ -1281,6 +1295,11 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
         }
       }
       __syncthreads();
+      if (P.dbg && tid == 0) {
+        const long long t = clock64();
+        dbg_b[2] += t - tb;
+        tb = t;
+      }
       // insertion: old position k -> k + (#selected before k); new point after k
       for (int k = tid; k < Lcur; k += ES_THREADS) {
         const int before = S.SCAN[k];
@@ -1291,6 +1310,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       for (int k = tid; k < Lcur + nsel; k += ES_THREADS) S.ORD[k] = S.ORD2[k];
       Lcur += nsel;
       __syncthreads();
+      if (P.dbg && tid == 0) dbg_b[3] += clock64() - tb;
     }
     const int L = Lcur;
     if (P.dbg && tid == 0) clk[2] = clock64();
@@ -1610,8 +1630,10 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     atomicOr(&sflags, flags);
     __syncthreads();
     if (tid == 0 && status) status[pi] = route ? (status[pi] | sflags) : sflags;
-    if (P.dbg)
+    if (P.dbg) {
       for (int k = tid; k < L; k += ES_THREADS) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + k] = S.TH[S.ORD[k]];
+      if (tid < 4) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + P.Lcap + tid] = (double)dbg_b[tid];
+    }
     __syncthreads();
   }
 }

@@ -63,8 +63,9 @@ typedef struct cgb_es_options {
   int32_t ld_group;       /* lanes sharing one contour point's quadrature nodes: 1, 2, 4 or 8 */
   int32_t labelling;      /* limb image row order: 0 = the reference's warm-start chain, reproduced
                              exactly (faithful FP64 solves on ambiguous steps); 1 = nearest-root
-                             matching everywhere (faster; the result moves within the reference's own
-                             sensitivity to its warm-start jitter, ~3e-5) */
+                             matching everywhere (faster; other gaps get refined where the reference
+                             would have labelled rows differently: up to 4e-4 measured, 6e-5 on the
+                             bench light curve) */
   double grad_fp64_above; /* mixed-precision adjoints: a contour point whose image tangents |dz/dtheta|
                              (own or neighbours', ~1/|det J|) exceed this runs its limb-darkening
                              quadrature in FP64; 0 = default (2), < 0 = every point in FP64 */
@@ -217,7 +218,9 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
  * [L, n_contours, merge flags, (start, count, parity, integral) x 13,
  *  clock cycles of the six phases, faithful-labelling solves of the initial
  *  chain (count + 1000 x iterations, first point included) and of the
- *  refinement (same encoding), theta of the L limb points in limb order]. */
+ *  refinement (same encoding), theta of the limb points in limb order (room
+ *  for the largest limb), clock cycles of the refinement's sub-phases: gaps,
+ *  ranking and scan; new-point solves; faithful labelling; insertion]. */
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                               const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
 int64_t cgb_debug_record_len(int32_t npts_limb);

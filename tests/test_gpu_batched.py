@@ -51,7 +51,9 @@ def test_batched_matches_single_curve_calls(precision):
         sl = slice(off[c], off[c + 1])
         w = traj(t[sl], cv[c])
         ref = C.mag(w, cv[c, 2], u1=cv[c, 3], s=cv[c, 0], q=cv[c, 1], precision=precision, **OPTS)
-        assert np.max(np.abs(m[sl] - ref) / ref) < 1e-12
+        # the batched pass evaluates the trajectory on the device, so source
+        # positions differ from the host's by ~1e-16
+        assert np.max(np.abs(m[sl] - ref) / ref) < (1e-12 if precision == "fp64" else 1e-10)
 
 
 def test_batched_vs_oracle():
