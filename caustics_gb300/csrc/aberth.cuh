@@ -293,6 +293,86 @@ __device__ int aberth64_comp(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bo
 // Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
 // polynomial, FP64 Newton polish, FP64 fallback.  Returns the FP32 iteration
 // count, -1 on non-convergence; sets CGB_ST_FALLBACK in flags when used.
+// The FP32 stages of aberth_mixed alone: FP32 Aberth, then the compensated
+// stage against the double-float coefficients.  z returns the FP32 roots;
+// the result says whether every root met the compensated stopping rule.
+template <int DEG>
+__device__ bool aberth_mixed_f32(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
+  cf ph[DEG + 1], pl[DEG + 1];
+  float alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) {
+    ph[i] = tof(p[i]);
+    pl[i] = tof(p[i] - tod(ph[i]));
+    alpha[i] = cabs(ph[i]);
+  }
+  if (!warm) init_estimates<DEG>(alpha, z);
+  cf zf[DEG];
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
+  const float gam = gamma_const<float>(4 * DEG + 2, CGB_EPS32);
+  uint32_t cx = 0, cy = 0;
+  const uint32_t all = (1u << DEG) - 1u;
+  int it = 0;
+  for (; it < itmax; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      float az = cabs(zf[j]);
+      bool rev = az > 1.0f;
+      cf x = rev ? crecip(zf[j]) : zf[j];
+      if (!((cx >> j) & 1u)) {
+        cf h, hd;
+        float b;
+        horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+        if (cabs(h) > CGB_EPS32 * b)
+          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
+        else
+          cx |= 1u << j;
+      } else if (!((cy >> j) & 1u)) {
+        cf h, hd;
+        float eb;
+        horner_comp<DEG, cf, float>(ph, pl, true, x, rev, h, hd, eb);
+        float ah = cabs(h);
+        float bound = CGB_EPS32 * ah + (gam * eb + 2 * CGB_EPS32 * CGB_EPS32 * ah);
+        if (ah > 4 * bound) {
+          cf c = aberth_corr<DEG>(zf, j, h, hd, rev);
+          if (cabs(c) > 4 * CGB_EPS32 * az)
+            zf[j] = zf[j] - c;
+          else
+            cy |= 1u << j;
+        } else {
+          cy |= 1u << j;
+        }
+      }
+    }
+    if (cy == all) break;
+  }
+  const bool ok = (cy == all) && isfinite(zf[0].x);
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) z[i] = tod(zf[i]);
+  return ok;
+}
+
+// FP64 Newton on one root of p (low -> high): at most 3 steps, done when a
+// correction is at most 2^-40 |z|.
+template <int DEG>
+__device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
+  for (int sweep = 0; sweep < 3; ++sweep) {
+    cd h = p[DEG], hd = mk(0, 0);
+#pragma unroll
+    for (int k = DEG - 1; k >= 0; --k) {
+      hd = cfma(hd, z, h);
+      h = cfma(h, z, p[k]);
+    }
+    const cd c = cdiv(h, hd);
+    z = z - c;
+    if (norm2(c) <= 8.271806125530277e-25 * fmax(norm2(z), 1e-300)) return true;
+  }
+  return false;
+}
+
 template <int DEG>
 __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
   cf ph[DEG + 1], pl[DEG + 1];

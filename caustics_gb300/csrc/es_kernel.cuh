@@ -189,8 +189,8 @@ __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, 
 #pragma unroll
   for (int i = 0; i < DEG; ++i) {
     zrow[i] = z[i];
-    const double r = cabs(lens_eq<NL>(I.L, z[i]) - w);
-    const double d = lens_det<NL>(I.L, z[i]);
+    double r, d;
+    lens_filter<NL>(I.L, z[i], w, r, d);
     if (r < 1e-6) mkb |= 1u << i;
     if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
     if (d > 0) pp |= 1u << i;
@@ -1006,6 +1006,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   __shared__ int nlist_sh;
   __shared__ int dbg_ref[5];  // diagnostics: first-point iterations; A: solves, iterations; B: solves, iterations
   __shared__ long long dbg_b[4];  // diagnostics: refinement clocks (gaps+rank+scan, solves, labelling, insertion)
+  __shared__ long long dbg_arr[ES_WARPS];  // diagnostics: each warp's clock on reaching a barrier
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
   __shared__ EsItem item;
@@ -1214,7 +1215,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     int Lcur = n0;
     long long tb = 0;
     for (int round = 0; round < P.niter; ++round) {
-      if (P.dbg && tid == 0) tb = clock64();
+      if (P.dbg && tid == 0 && round == 0) tb = clock64();
       const int ngap = Lcur - 1;
       for (int k = tid; k < ngap; k += ES_THREADS) {
         const int s1 = S.ORD[k], s2 = S.ORD[k + 1];
@@ -1245,13 +1246,131 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       // positions of the selected gaps -> compact list in SCAN (exclusive scan)
       for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
       __syncthreads();
-      int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);
+      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
+      int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);  // synchronises the block
+      // each sub-phase ends when its last warp reaches the closing barrier
+      auto last_arrival = [&]() {
+        long long m = dbg_arr[0];
+        for (int q = 1; q < ES_WARPS; ++q) m = max(m, dbg_arr[q]);
+        return m;
+      };
       if (P.dbg && tid == 0) {
-        const long long t = clock64();
+        const long long t = last_arrival();
         dbg_b[0] += t - tb;
         tb = t;
       }
+      if (P.dbg) __syncthreads();  // keep the arrival clocks until read
       // new slots: selected gap k -> slot Lcur + SCAN[k]
+      if (PREC == MIXED) {
+        // One new point per thread leaves a single warp doing the FP64 polish
+        // and image filter of every root in turn, which made these solves the
+        // longest path of the refinement; here the FP32 stages run per point,
+        // then one lane per (point, root) polishes and filters, then one thread
+        // per point checks the root set and labels it.  Scratch lives in the
+        // candidate lists' storage, unused until the chained matching.
+        cd *pco = reinterpret_cast<cd *>(S.CAND);  // [nsel][DEG + 2]: coefficients, then w
+        uint32_t *rflag = reinterpret_cast<uint32_t *>(pco + (size_t)nsel * (DEG + 2));  // [nsel][DEG]
+        int *pok = reinterpret_cast<int *>(rflag + (size_t)nsel * DEG);                  // [nsel]
+        int *psl = pok + nsel;                                                           // [nsel]
+        for (int k = tid; k < ngap; k += ES_THREADS) {
+          if (S.KEY[k] == 0.0) continue;
+          const int j = S.SCAN[k], slot = Lcur + j;
+          const int sl = S.ORD[k], sr = S.ORD[k + 1];
+          const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
+          S.TH[slot] = th;
+          psl[j] = sl;
+          double sn, cs;
+          sincos(th, &sn, &cs);
+          const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
+          cd p[DEG + 1], z[DEG];
+          lens_poly<NL>(I.L, w, p);
+          // warm start from the left neighbour's rows with the fixed jitter
+          // (extended_source.py:79-98, 128-129)
+#pragma unroll
+          for (int i = 0; i < DEG; ++i)
+            z[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
+          pok[j] = aberth_mixed_f32<DEG>(p, z, P.itmax, true) ? 1 : 0;
+#pragma unroll
+          for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
+          pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
+#pragma unroll
+          for (int i = 0; i < DEG; ++i) S.Z[(size_t)slot * DEG + i] = z[i];
+        }
+        __syncthreads();
+        for (int idx = tid; idx < nsel * DEG; idx += ES_THREADS) {
+          const int j = idx / DEG, i = idx - j * DEG, slot = Lcur + j;
+          uint32_t f = 0;
+          if (pok[j]) {
+            cd p[DEG + 1];
+#pragma unroll
+            for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
+            cd z = S.Z[(size_t)slot * DEG + i];
+            if (newton_polish_root<DEG>(p, z)) f |= 1u;
+            S.Z[(size_t)slot * DEG + i] = z;
+            double r, d;
+            lens_filter<NL>(I.L, z, pco[(size_t)j * (DEG + 2) + DEG + 1], r, d);
+            if (r < 1e-6) f |= 2u;
+            if (d > 0) f |= 4u;
+            if (d == 0) f |= 8u;
+            if (r > 1e-6 / 30 && r < 1e-6 * 30) f |= 16u;
+          }
+          rflag[idx] = f;
+        }
+        __syncthreads();
+        for (int j = tid; j < nsel; j += ES_THREADS) {
+          const int slot = Lcur + j, sl = psl[j];
+          cd *zrow = S.Z + (size_t)slot * DEG;
+          bool ok = pok[j] != 0;
+#pragma unroll
+          for (int i = 0; i < DEG; ++i) ok = ok && (rflag[j * DEG + i] & 1u);
+          if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
+            double scale = 0.0;
+            for (int i = 0; i < DEG; ++i) scale = fmax(scale, norm2(zrow[i]));
+            for (int i = 0; i < DEG; ++i)
+              for (int q = i + 1; q < DEG; ++q)
+                if (norm2(zrow[i] - zrow[q]) < 1e-14 * scale) ok = false;
+          }
+          uint16_t mkb = 0, pp = 0, zp = 0;
+          if (ok) {
+            for (int i = 0; i < DEG; ++i) {
+              const uint32_t f = rflag[j * DEG + i];
+              mkb |= (uint16_t)(((f >> 1) & 1u) << i);
+              pp |= (uint16_t)(((f >> 2) & 1u) << i);
+              zp |= (uint16_t)(((f >> 3) & 1u) << i);
+              if (f & 16u) flags |= CGB_ST_AMBIGUOUS;
+            }
+          } else {  // the mixed solver's FP64 fallback, then the filter here
+            flags |= CGB_ST_FALLBACK;
+            cd p[DEG + 1], z[DEG];
+#pragma unroll
+            for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
+#pragma unroll
+            for (int i = 0; i < DEG; ++i) z[i] = zrow[i];
+            if (aberth64<DEG>(p, z, P.itmax, true) < 0 && aberth64<DEG>(p, z, P.itmax, false) < 0)
+              flags |= CGB_ST_NOCONV;
+            const cd w = pco[(size_t)j * (DEG + 2) + DEG + 1];
+#pragma unroll
+            for (int i = 0; i < DEG; ++i) {
+              zrow[i] = z[i];
+              double r, d;
+              lens_filter<NL>(I.L, z[i], w, r, d);
+              if (r < 1e-6) mkb |= 1u << i;
+              if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
+              if (d > 0) pp |= 1u << i;
+              if (d == 0) zp |= 1u << i;
+            }
+          }
+          S.MK[slot] = mkb;
+          S.PP[slot] = pp;
+          S.ZP[slot] = zp;
+          bool amb;
+          const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, zrow, amb);
+          if (amb && !P.nearest)  // labelled below by the reference's warm start, on a lane group
+            S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
+          else
+            apply_rows<DEG>(zrow, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+        }
+      } else
       for (int k = tid; k < ngap; k += ES_THREADS) {
         if (S.KEY[k] != 0.0) {
           const int j = S.SCAN[k];
@@ -1271,12 +1390,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
             apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
         }
       }
+      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
       if (P.dbg && tid == 0) {
-        const long long t = clock64();
+        const long long t = last_arrival();
         dbg_b[1] += t - tb;
         tb = t;
       }
+      if (P.dbg) __syncthreads();  // keep the arrival clocks until read
       {
         uint64_t ident = 0;
         for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
@@ -1294,12 +1415,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           }
         }
       }
+      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
       if (P.dbg && tid == 0) {
-        const long long t = clock64();
+        const long long t = last_arrival();
         dbg_b[2] += t - tb;
         tb = t;
       }
+      if (P.dbg) __syncthreads();  // keep the arrival clocks until read
       // insertion: old position k -> k + (#selected before k); new point after k
       for (int k = tid; k < Lcur; k += ES_THREADS) {
         const int before = S.SCAN[k];
@@ -1309,8 +1432,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       __syncthreads();
       for (int k = tid; k < Lcur + nsel; k += ES_THREADS) S.ORD[k] = S.ORD2[k];
       Lcur += nsel;
+      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
-      if (P.dbg && tid == 0) dbg_b[3] += clock64() - tb;
+      if (P.dbg && tid == 0) {
+        const long long t = last_arrival();
+        dbg_b[3] += t - tb;
+        tb = t;
+      }
+      if (P.dbg) __syncthreads();
     }
     const int L = Lcur;
     if (P.dbg && tid == 0) clk[2] = clock64();

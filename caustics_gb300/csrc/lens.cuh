@@ -148,6 +148,23 @@ __device__ __forceinline__ cd lens_eq(const Lens &L, cd z) {
   return w;
 }
 
+// Image filter of one root: resid = |lens_eq(z) - w| and det = det J, with the
+// reciprocals 1 / (conj(z) - conj(r_j)) shared; each quantity is accumulated in
+// the same order as lens_eq and lens_det, so both agree with them bit for bit.
+template <int NL>
+__device__ __forceinline__ void lens_filter(const Lens &L, cd z, cd w, double &resid, double &det) {
+  const cd zb = conj(z);
+  cd weq = z, lam = mk(0, 0);
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    const cd t = crecip(zb - conj(L.r[j]));
+    weq = weq - t * L.eps[j];
+    lam = lam + t * t * L.eps[j];
+  }
+  resid = cabs(weq - w);
+  det = 1.0 - norm2(lam);
+}
+
 // det J = 1 - |sum_j eps_j / (conj(z) - conj(r_j))^2|^2   (point_source.py:1558-1580)
 template <int NL>
 __device__ __forceinline__ double lens_det(const Lens &L, cd z) {
