@@ -198,7 +198,7 @@ __device__ __forceinline__ void horner_comp(const C (&p)[DEG + 1], const C (&pl)
   C H = rev ? p[0] : p[DEG];
   C e = use_lo ? (rev ? pl[0] : pl[DEG]) : H - H;
   C D = H - H, ed = H - H;
-  R ax = sqrt(x.x * x.x + x.y * x.y);
+  R ax = msqrt(x.x * x.x + x.y * x.y);
   eb = 0;
 #pragma unroll
   for (int k = 1; k <= DEG; ++k) {
@@ -228,7 +228,7 @@ __device__ __forceinline__ void horner_comp(const C (&p)[DEG + 1], const C (&pl)
     C lo = C{(q0 - q1) + (r4 + ex), (q2 + q3) + (r5 + ey)};
     if (use_lo) lo = lo + (rev ? pl[k] : pl[DEG - k]);
     e = cfma(e, x, lo);
-    eb = eb * ax + (fabs(q0) + fabs(q1) + fabs(q2) + fabs(q3) + fabs(r4) + fabs(r5) + fabs(ex) + fabs(ey));
+    eb = eb * ax + (mabs(q0) + mabs(q1) + mabs(q2) + mabs(q3) + mabs(r4) + mabs(r5) + mabs(ex) + mabs(ey));
   }
   h_out = H + e;
   hd_out = D + ed;
@@ -296,8 +296,10 @@ __device__ int aberth64_comp(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bo
 // The FP32 stages of aberth_mixed alone: FP32 Aberth, then the compensated
 // stage against the double-float coefficients.  z returns the FP32 roots;
 // the result says whether every root met the compensated stopping rule.
-template <int DEG>
-__device__ bool aberth_mixed_f32(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm) {
+// COMP = false stops after the plain FP32 stage (every root meets the FP32
+// stopping rule), for callers that polish every root in FP64 right after.
+template <int DEG, bool COMP = true>
+__device__ bool aberth_mixed_f32(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, int *iters = nullptr) {
   cf ph[DEG + 1], pl[DEG + 1];
   float alpha[DEG + 1];
 #pragma unroll
@@ -347,19 +349,20 @@ __device__ bool aberth_mixed_f32(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax
         }
       }
     }
-    if (cy == all) break;
+    if (cy == all || (!COMP && cx == all)) break;
   }
-  const bool ok = (cy == all) && isfinite(zf[0].x);
+  const bool ok = (COMP ? cy == all : cx == all) && isfinite(zf[0].x);
 #pragma unroll
   for (int i = 0; i < DEG; ++i) z[i] = tod(zf[i]);
+  if (iters) *iters = it + 1;
   return ok;
 }
 
-// FP64 Newton on one root of p (low -> high): at most 3 steps, done when a
+// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
 // correction is at most 2^-40 |z|.
-template <int DEG>
+template <int DEG, int SWEEPS = 3>
 __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
-  for (int sweep = 0; sweep < 3; ++sweep) {
+  for (int sweep = 0; sweep < SWEEPS; ++sweep) {
     cd h = p[DEG], hd = mk(0, 0);
 #pragma unroll
     for (int k = DEG - 1; k >= 0; --k) {

@@ -63,6 +63,14 @@ CGB_HD cf cfma(cf a, cf b, cf c) {
   return cf{fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y))};
 }
 
+// square root and absolute value in the argument's own precision (templated
+// code must never widen an FP32 quantity to FP64: on GB300 the FP64 pipe is
+// ~60x narrower)
+CGB_HD float msqrt(float x) { return sqrtf(x); }
+CGB_HD double msqrt(double x) { return sqrt(x); }
+CGB_HD float mabs(float x) { return fabsf(x); }
+CGB_HD double mabs(double x) { return fabs(x); }
+
 // ---- error-free transformations (Knuth TwoSum, FMA-based TwoProd) ----
 template <typename T>
 CGB_HD void two_sum(T a, T b, T &s, T &e) {

@@ -752,12 +752,12 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         const R r = cabs(srho);
         R B, dB;
         if (x1 >= (R)0) {
-          const R sq = sqrt(x1);
+          const R sq = msqrt(x1);
           B = (R)1 + sq;
           dB = x1 > (R)0 ? -r / sq : (R)0;
         } else {
           const R r2 = r * r, x = -x1 / r2;  // 1 - 1/r^2
-          const R sq = sqrt(x);
+          const R sq = msqrt(x);
           B = (R)1 - sq;
           dB = -(R)1 / (r2 * r * sq);
         }
@@ -1004,8 +1004,10 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   __shared__ uint32_t sflags;
   __shared__ int nsel_sh;
   __shared__ int nlist_sh;
-  __shared__ int dbg_ref[5];  // diagnostics: first-point iterations; A: solves, iterations; B: solves, iterations
-  __shared__ long long dbg_b[4];  // diagnostics: refinement clocks (gaps+rank+scan, solves, labelling, insertion)
+  __shared__ int dbg_ref[7];  // diagnostics: first-point iterations; A: solves, iterations; B: solves,
+                             // iterations; refinement FP32-stage iterations, refinement points
+  __shared__ long long dbg_b[ES_DBG_SUB];  // diagnostics: refinement clocks (gaps+rank+scan, FP32 stages or
+                                           // whole solves, polish + filter, per-point labelling, faithful, insertion)
   __shared__ long long dbg_arr[ES_WARPS];  // diagnostics: each warp's clock on reaching a barrier
   __shared__ long long clk[8];
   __shared__ int64_t item_sh;
@@ -1118,8 +1120,8 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     const EsItem &I = item;
     if (P.dbg && tid == 0) {
       clk[0] = clock64();
-      for (int c = 0; c < 5; ++c) dbg_ref[c] = 0;
-      for (int c = 0; c < 4; ++c) dbg_b[c] = 0;
+      for (int c = 0; c < 7; ++c) dbg_ref[c] = 0;
+      for (int c = 0; c < ES_DBG_SUB; ++c) dbg_b[c] = 0;
     }
 
     // ---- A: initial limb sampling (extended_source.py:100-107) ----
@@ -1133,7 +1135,19 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       S.ORD[k] = (uint16_t)k;
       solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)k * DEG, nullptr, S.MK[k], S.PP[k], S.ZP[k], flags);
     }
+    if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
     __syncthreads();
+    long long ta = 0;  // diagnostics: end of the previous initial-sampling sub-phase (thread 0)
+    auto arrival_max = [&]() {
+      long long m = dbg_arr[0];
+      for (int q = 1; q < ES_WARPS; ++q) m = max(m, dbg_arr[q]);
+      return m;
+    };
+    if (P.dbg && tid == 0) {
+      ta = arrival_max();
+      dbg_b[6] += ta - clk[0];
+    }
+    if (P.dbg) __syncthreads();
     // Row order of the reference's sequential warm-start chain, emulated in
     // parallel: clear steps take the nearest-root map; ambiguous steps rerun the
     // reference's warm start from the predecessor in the current chain order,
@@ -1158,7 +1172,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       S.BMAP[k] = step_map<DEG>(S.Z + (size_t)(k - 1) * DEG, S.Z + (size_t)k * DEG, amb);
       S.USED[k] = (amb && !P.nearest) ? ~0ull : 0ull;  // 0: map final (clear step, or nearest labelling)
     }
+    if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
     __syncthreads();
+    if (P.dbg && tid == 0) {
+      const long long t = arrival_max();
+      dbg_b[7] += t - ta;
+      ta = t;
+    }
+    if (P.dbg) __syncthreads();
     for (int round = 0; round < 12; ++round) {
       if (tid == 0) {
         uint64_t ord = S.PERM[0];
@@ -1208,7 +1229,10 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     }
     for (int k = tid; k < n0; k += ES_THREADS)
       apply_rows<DEG>(S.Z + (size_t)k * DEG, S.MK[k], S.PP[k], S.ZP[k], S.PERM[k]);
+    if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
     __syncthreads();
+    if (P.dbg && tid == 0) dbg_b[8] += arrival_max() - ta;
+    if (P.dbg) __syncthreads();
     if (P.dbg && tid == 0) clk[1] = clock64();
 
     // ---- B: refinement rounds (extended_source.py:109-135) ----
@@ -1289,14 +1313,29 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
 #pragma unroll
           for (int i = 0; i < DEG; ++i)
             z[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
-          pok[j] = aberth_mixed_f32<DEG>(p, z, P.itmax, true) ? 1 : 0;
+          int its = 0;
+          // plain FP32 stage only: every root gets up to 5 FP64 Newton steps next,
+          // on its own lane, which costs less than the compensated FP32 stage
+          // run root after root on one thread
+          pok[j] = aberth_mixed_f32<DEG, false>(p, z, P.itmax, true, &its) ? 1 : 0;
+          if (P.dbg) {
+            atomicAdd(&dbg_ref[5], its);
+            atomicAdd(&dbg_ref[6], 1);
+          }
 #pragma unroll
           for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
           pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
 #pragma unroll
           for (int i = 0; i < DEG; ++i) S.Z[(size_t)slot * DEG + i] = z[i];
         }
+        if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
         __syncthreads();
+        if (P.dbg && tid == 0) {
+          const long long t = last_arrival();
+          dbg_b[1] += t - tb;
+          tb = t;
+        }
+        if (P.dbg) __syncthreads();
         for (int idx = tid; idx < nsel * DEG; idx += ES_THREADS) {
           const int j = idx / DEG, i = idx - j * DEG, slot = Lcur + j;
           uint32_t f = 0;
@@ -1305,7 +1344,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
 #pragma unroll
             for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
             cd z = S.Z[(size_t)slot * DEG + i];
-            if (newton_polish_root<DEG>(p, z)) f |= 1u;
+            if (newton_polish_root<DEG, 5>(p, z)) f |= 1u;
             S.Z[(size_t)slot * DEG + i] = z;
             double r, d;
             lens_filter<NL>(I.L, z, pco[(size_t)j * (DEG + 2) + DEG + 1], r, d);
@@ -1316,7 +1355,14 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           }
           rflag[idx] = f;
         }
+        if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
         __syncthreads();
+        if (P.dbg && tid == 0) {
+          const long long t = last_arrival();
+          dbg_b[2] += t - tb;
+          tb = t;
+        }
+        if (P.dbg) __syncthreads();
         for (int j = tid; j < nsel; j += ES_THREADS) {
           const int slot = Lcur + j, sl = psl[j];
           cd *zrow = S.Z + (size_t)slot * DEG;
@@ -1394,7 +1440,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       __syncthreads();
       if (P.dbg && tid == 0) {
         const long long t = last_arrival();
-        dbg_b[1] += t - tb;
+        dbg_b[PREC == MIXED ? 3 : 1] += t - tb;
         tb = t;
       }
       if (P.dbg) __syncthreads();  // keep the arrival clocks until read
@@ -1419,7 +1465,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       __syncthreads();
       if (P.dbg && tid == 0) {
         const long long t = last_arrival();
-        dbg_b[2] += t - tb;
+        dbg_b[4] += t - tb;
         tb = t;
       }
       if (P.dbg) __syncthreads();  // keep the arrival clocks until read
@@ -1436,7 +1482,7 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
       __syncthreads();
       if (P.dbg && tid == 0) {
         const long long t = last_arrival();
-        dbg_b[3] += t - tb;
+        dbg_b[5] += t - tb;
         tb = t;
       }
       if (P.dbg) __syncthreads();
@@ -1761,7 +1807,8 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     if (tid == 0 && status) status[pi] = route ? (status[pi] | sflags) : sflags;
     if (P.dbg) {
       for (int k = tid; k < L; k += ES_THREADS) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + k] = S.TH[S.ORD[k]];
-      if (tid < 4) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + P.Lcap + tid] = (double)dbg_b[tid];
+      if (tid < ES_DBG_SUB) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + P.Lcap + tid] = (double)dbg_b[tid];
+      if (tid < 2) P.dbg[(size_t)pi * ES_DBG_STRIDE(P.Lcap) + ES_DBG_HEAD + P.Lcap + ES_DBG_SUB + tid] = dbg_ref[5 + tid];
     }
     __syncthreads();
   }
