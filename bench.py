@@ -39,6 +39,11 @@ UNIT = "evals/s"
 # nominal FP64-equivalent work of one full contour evaluation at npts_limb=L,
 # npts_ld=G: L root solves (5.7e3 flop) + ~3.1 L contour points x 2G nodes x 60 flop
 FLOP_PER_EVAL = WL["npts_limb"] * 5.7e3 + 3.1 * WL["npts_limb"] * WL["npts_ld"] * 2 * 60
+# DRAM bytes (read + write) per evaluation of the contour kernel, from one ncu
+# capture of a 300-evaluation launch of this workload (1.95 MB per launch;
+# instruction, constant and register-spill traffic: the inputs are 24 B per
+# evaluation), scaled by the evaluations of a launch
+DRAM_BYTES_PER_EVAL = 1.954e6 / 300
 
 
 def trajectory(n):
@@ -426,7 +431,9 @@ def main():
         "config": {**WL, "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas",
                    "autotuned": ev.config, "cuda_graph": ev.graph is not None},
         "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None, "kernel": "es_kernel<2,MIXED>",
+                     "frac": achieved / fp32_peak, "traffic": DRAM_BYTES_PER_EVAL * WL["npoints"],
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 300-evaluation launch, "
+                                       "scaled to this launch's evaluations", "kernel": "es_kernel<2,MIXED>",
                      "peak_source": "measured live in bench.py (cgb_probe_fma, FP32 FMA burst); the path moves "
                                     "24 B per evaluation, so neither HBM nor tensor peaks bound it",
                      "flop_per_eval": FLOP_PER_EVAL,

@@ -71,7 +71,6 @@ struct EsSmem {
   uint64_t *BMAP; // [Lcap] warm-start map of the limb chain: root of k-1 -> root of k
   uint64_t *USED; // [Lcap] chain order of k-1 the map was computed with
   uint64_t *CAND; // [Lcap * DEG] candidate rows of position k sorted by distance, per row of k-1
-  cd *PQ;         // [CPcap] adjoint: (P_i, Q_i) per contour point
   cd *GG;         // [CPcap] adjoint: dT/dx_i + i dT/dy_i per contour point
   double *KEY;    // [Lcap]
   int *SCAN;      // [Lcap + 1]
@@ -990,7 +989,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
 }
 
 template <int NL, int PREC, bool GRAD = false>
-__global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
+__global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                         const int64_t *__restrict__ index,
                                                         const uint8_t *__restrict__ route, int64_t npoints,
                                                         double *__restrict__ mag, uint32_t *__restrict__ status) {
@@ -1018,11 +1017,18 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
   const int Lcap = P.Lcap;
   EsSmem<DEG> S;
   {
+    // Z, TH and CP stay live through the integrals and the adjoint; everything
+    // after them is dead once the contour point lists exist, so the adjoint's
+    // per-point accumulators GG reuse that region when it is large enough.
     unsigned char *p = smem_raw;
     S.Z = reinterpret_cast<cd *>(p);
     p += sizeof(cd) * (size_t)Lcap * DEG;
     S.TH = reinterpret_cast<double *>(p);
     p += sizeof(double) * Lcap;
+    S.CP = reinterpret_cast<uint32_t *>(p);
+    p += sizeof(uint32_t) * (size_t)P.CPcap;
+    p = smem_raw + (((size_t)(p - smem_raw) + 15) / 16 * 16);
+    unsigned char *const dead = p;
     S.KEY = reinterpret_cast<double *>(p);
     p += sizeof(double) * Lcap;
     S.PERM = reinterpret_cast<uint64_t *>(p);
@@ -1035,8 +1041,6 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     p += sizeof(uint64_t) * (size_t)Lcap * DEG;
     S.M = reinterpret_cast<MergeState *>(p);
     p += (sizeof(MergeState) + 15) / 16 * 16;
-    S.CP = reinterpret_cast<uint32_t *>(p);
-    p += sizeof(uint32_t) * (size_t)P.CPcap;
     S.SCAN = reinterpret_cast<int *>(p);
     p += sizeof(int) * (Lcap + 1);
     S.MK = reinterpret_cast<uint16_t *>(p);
@@ -1050,9 +1054,8 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
     S.ORD2 = reinterpret_cast<uint16_t *>(p);
     p += sizeof(uint16_t) * Lcap;
     p = smem_raw + (((size_t)(p - smem_raw) + 15) / 16 * 16);
-    S.PQ = reinterpret_cast<cd *>(p);
-    p += sizeof(cd) * (size_t)P.CPcap;
-    S.GG = reinterpret_cast<cd *>(p);
+    S.GG = ((size_t)(p - dead) >= sizeof(cd) * (size_t)P.CPcap) ? reinterpret_cast<cd *>(dead)
+                                                                  : reinterpret_cast<cd *>(p);
   }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -1757,7 +1760,6 @@ __global__ void __launch_bounds__(ES_THREADS, (NL == 2 && !GRAD) ? 2 : 1) es_ker
           pq.y += __shfl_xor_sync(0xffffffffu, pq.y, o);
         }
         if (valid && r == 0) {
-          if (GRAD) S.PQ[i] = pq;
           atomicAdd(&contour_acc[warp][c], pq.x * wx + pq.y * wy);
         }
       }

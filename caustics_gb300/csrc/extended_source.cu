@@ -62,18 +62,25 @@ cudaError_t launch_es_grad(const EsParams &P, const double *w0, const uint8_t *r
 }
 
 size_t es_smem_bytes(const EsParams &P, int nl, bool grad) {
+  // must follow the layout in es_kernel (es_kernel.cuh)
   const int deg = nl * nl + 1;
-  size_t b = 0;
-  b += sizeof(cd) * (size_t)P.Lcap * deg;
-  b += sizeof(double) * P.Lcap * 2;
-  b += sizeof(uint64_t) * P.Lcap * (3 + deg);
-  b += (sizeof(MergeState) + 15) / 16 * 16;
-  b += sizeof(uint32_t) * (size_t)P.CPcap;
-  b += sizeof(int) * (P.Lcap + 1);
-  b += sizeof(uint16_t) * P.Lcap * 5;
-  b = (b + 15) / 16 * 16;
-  if (grad) b += 2 * sizeof(cd) * (size_t)P.CPcap;  // P/Q values and dT/dz per contour point
-  return (b + 15) / 16 * 16;
+  auto up16 = [](size_t v) { return (v + 15) / 16 * 16; };
+  size_t live = 0;
+  live += sizeof(cd) * (size_t)P.Lcap * deg;
+  live += sizeof(double) * P.Lcap;
+  live += sizeof(uint32_t) * (size_t)P.CPcap;
+  live = up16(live);
+  size_t dead = 0;
+  dead += sizeof(double) * P.Lcap;
+  dead += sizeof(uint64_t) * P.Lcap * (3 + deg);
+  dead += (sizeof(MergeState) + 15) / 16 * 16;
+  dead += sizeof(int) * (P.Lcap + 1);
+  dead += sizeof(uint16_t) * P.Lcap * 5;
+  dead = up16(live + dead) - live;
+  const size_t gg = sizeof(cd) * (size_t)P.CPcap;
+  size_t b = live + dead;
+  if (grad && dead < gg) b += gg;  // the adjoint's accumulators reuse the dead region when it is large enough
+  return up16(b);
 }
 
 }  // namespace cgb
