@@ -296,6 +296,42 @@ __device__ int aberth64_comp(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bo
 // The FP32 stages of aberth_mixed alone: FP32 Aberth, then the compensated
 // stage against the double-float coefficients.  z returns the FP32 roots;
 // the result says whether every root met the compensated stopping rule.
+// No two roots closer than 1e-7 of the largest root's modulus.  A root set
+// that fails this is not trusted (two starts may have converged onto one root,
+// leaving another root unfound).
+template <int DEG>
+__device__ __forceinline__ bool roots_distinct(const cd (&z)[DEG]) {
+  double scale = 0.0;
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) scale = fmax(scale, norm2(z[i]));
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < DEG; ++i)
+#pragma unroll
+    for (int k = i + 1; k < DEG; ++k)
+      if (norm2(z[i] - z[k]) < 1e-14 * scale) ok = false;
+  return ok;
+}
+
+// FP64 fallback of the mixed solver.  It never warm-starts from a set with
+// merged roots: with two coincident starts the Aberth correction of the pair
+// degenerates and both can settle on one root.  warm (if given) is a start known
+// to separate the roots (e.g. the neighbouring limb point's roots plus jitter);
+// otherwise, or if that fails or merges roots, a cold start.  Returns the FP64
+// iteration count or -1.
+template <int DEG>
+__device__ int aberth64_fallback(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, const cd *warm) {
+  int it = -1;
+  if (warm) {
+#pragma unroll
+    for (int i = 0; i < DEG; ++i) z[i] = warm[i];
+    it = aberth64<DEG>(p, z, itmax, true);
+    if (it >= 0 && roots_distinct<DEG>(z)) return it;
+  }
+  it = aberth64<DEG>(p, z, itmax, false);
+  return (it >= 0 && roots_distinct<DEG>(z)) ? it : -1;
+}
+
 // COMP = false stops after the plain FP32 stage (every root meets the FP32
 // stopping rule), for callers that polish every root in FP64 right after.
 template <int DEG, bool COMP = true>
@@ -466,12 +502,7 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   }
   if (!ok) {
     flags |= CGB_ST_FALLBACK;
-    int it64 = aberth64<DEG>(p, z, itmax, true);
-    if (it64 < 0) {
-      // restart cold in FP64 once before reporting failure
-      it64 = aberth64<DEG>(p, z, itmax, false);
-      if (it64 < 0) return -1;
-    }
+    if (aberth64_fallback<DEG>(p, z, itmax, nullptr) < 0) return -1;
   }
   return it + 1;
 }

@@ -608,6 +608,27 @@ __device__ cd ld_point_fp64(const EsParams &P, const EsItem &It, cd zc, cd z0, i
   return mk(-0.5 * acc[0], 0.5 * acc[1]);  // (P_i, Q_i)
 }
 
+// Node arithmetic of the FP32 quadrature: approximate reciprocal (at most 2
+// ulp, one special-function instruction) and square root through rsqrt; each
+// node's FP32 value carries ~1e-7 relative error either way.
+__device__ __forceinline__ cf crecip_fast(cf b) {
+  const float inv = __fdividef(1.0f, b.x * b.x + b.y * b.y);
+  return cf{b.x * inv, -b.y * inv};
+}
+__device__ __forceinline__ float cabs_fast(cf a) {
+  const float n = a.x * a.x + a.y * a.y;
+  return n > 0.0f ? n * rsqrtf(n) : 0.0f;
+}
+__device__ __forceinline__ float brightness_bf_fast(float r) {
+  // B(r) = 1 + sqrt(1 - r^2) inside the limb, 1 - sqrt(1 - 1/r^2) outside
+  if (r <= 1.0f) {
+    const float x = fmaxf(1.0f - r * r, 0.0f);
+    return 1.0f + (x > 0.0f ? x * rsqrtf(x) : 0.0f);
+  }
+  const float x = fmaxf(1.0f - __fdividef(1.0f, r * r), 0.0f);
+  return 1.0f - (x > 0.0f ? x * rsqrtf(x) : 0.0f);
+}
+
 // FP32 nodes on a shifted lens equation:
 //   lens_eq(zc + d) - w0 = (lens_eq(zc) - w0) + d + sum_j eps_j conj(d) / (D_j (D_j + conj(d))),
 //   D_j = conj(zc) - conj(r_j);
@@ -648,11 +669,11 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0, 
 #pragma unroll
         for (int k = 0; k < NL; ++k) {
           const cf den = cfma(Dj[k], cdl, Dj2[k]);  // D (D + conj(delta))
-          const cf t = cdl * crecip(den);
+          const cf t = cdl * crecip_fast(den);
           sacc = sacc + t * ej[k];
         }
-        const float r = cabs(sacc);
-        const float I = c0 * (u1 * brightness_bf(r) + 1.0f - 2.0f * u1);
+        const float r = cabs_fast(sacc);
+        const float I = c0 * (u1 * brightness_bf_fast(r) + 1.0f - 2.0f * u1);
         sum = fmaf((float)P.gl_w[half][j], I, sum);
       }
       acc[isQ] += (double)hw * (double)sum;
@@ -1373,11 +1394,10 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
 #pragma unroll
           for (int i = 0; i < DEG; ++i) ok = ok && (rflag[j * DEG + i] & 1u);
           if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
-            double scale = 0.0;
-            for (int i = 0; i < DEG; ++i) scale = fmax(scale, norm2(zrow[i]));
-            for (int i = 0; i < DEG; ++i)
-              for (int q = i + 1; q < DEG; ++q)
-                if (norm2(zrow[i] - zrow[q]) < 1e-14 * scale) ok = false;
+            cd zz[DEG];
+#pragma unroll
+            for (int i = 0; i < DEG; ++i) zz[i] = zrow[i];
+            ok = roots_distinct<DEG>(zz);
           }
           uint16_t mkb = 0, pp = 0, zp = 0;
           if (ok) {
@@ -1390,13 +1410,14 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
             }
           } else {  // the mixed solver's FP64 fallback, then the filter here
             flags |= CGB_ST_FALLBACK;
-            cd p[DEG + 1], z[DEG];
+            cd p[DEG + 1], z[DEG], warm[DEG];
 #pragma unroll
             for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
+            // the FP64 path's own start: the left neighbour's roots plus the jitter
 #pragma unroll
-            for (int i = 0; i < DEG; ++i) z[i] = zrow[i];
-            if (aberth64<DEG>(p, z, P.itmax, true) < 0 && aberth64<DEG>(p, z, P.itmax, false) < 0)
-              flags |= CGB_ST_NOCONV;
+            for (int i = 0; i < DEG; ++i)
+              warm[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
+            if (aberth64_fallback<DEG>(p, z, P.itmax, warm) < 0) flags |= CGB_ST_NOCONV;
             const cd w = pco[(size_t)j * (DEG + 2) + DEG + 1];
 #pragma unroll
             for (int i = 0; i < DEG; ++i) {

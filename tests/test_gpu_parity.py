@@ -208,3 +208,19 @@ def test_empty_inputs():
     assert C.mag_point_source(np.zeros(0, dtype=complex), s=1.0, q=0.1).shape == (0,)
     assert C.mag_extended_source(np.zeros(0, dtype=complex), 0.01, s=1.0, q=0.1).shape == (0,)
     assert C.mag(np.zeros(0, dtype=complex), 0.01, s=1.0, q=0.1).shape == (0,)
+
+
+def test_mixed_fallback_near_double_root():
+    """A limb whose images include a near-double pair (residuals ~5e-11): the
+    mixed solver's Newton steps can merge the pair; its FP64 fallback must not
+    warm-start from the merged set (the Aberth correction of two coincident
+    starts degenerates and one root stays unfound).  A point of the 4096-curve
+    batched workload (seed 2) where that once moved the result by 1.6e-4."""
+    kw = dict(npts_limb=200, limb_darkening=True, u1=0.48632774435103615, npts_ld=100, s=2.012958725668278,
+              q=0.0011055346801834944)
+    w = np.array([-1.4724702703191945 + 0.004269936791693629j])
+    m64 = C.mag_extended_source(w, 0.028097114572181326, precision="fp64", **kw)
+    m32 = C.mag_extended_source(w, 0.028097114572181326, precision="mixed", **kw)
+    ref = O.mag_extended_source(w[0], 0.028097114572181326, **kw)
+    assert abs(m64[0] - ref) / ref < 1e-9
+    assert abs(m32[0] - ref) / ref < 1e-6
