@@ -40,10 +40,10 @@ UNIT = "evals/s"
 # npts_ld=G: L root solves (5.7e3 flop) + ~3.1 L contour points x 2G nodes x 60 flop
 FLOP_PER_EVAL = WL["npts_limb"] * 5.7e3 + 3.1 * WL["npts_limb"] * WL["npts_ld"] * 2 * 60
 # DRAM bytes (read + write) per evaluation of the contour kernel, from one ncu
-# capture of a 300-evaluation launch of this workload (1.95 MB per launch;
+# capture of a 300-evaluation launch of this workload (1.73 MB per launch;
 # instruction, constant and register-spill traffic: the inputs are 24 B per
 # evaluation), scaled by the evaluations of a launch
-DRAM_BYTES_PER_EVAL = 1.954e6 / 300
+DRAM_BYTES_PER_EVAL = 1.730e6 / 300
 
 
 def trajectory(n):
