@@ -1330,27 +1330,82 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           double sn, cs;
           sincos(th, &sn, &cs);
           const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
-          cd p[DEG + 1], z[DEG];
+          cd p[DEG + 1];
           lens_poly<NL>(I.L, w, p);
+#pragma unroll
+          for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
+          pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
           // warm start from the left neighbour's rows with the fixed jitter
           // (extended_source.py:79-98, 128-129)
 #pragma unroll
           for (int i = 0; i < DEG; ++i)
-            z[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
-          int its = 0;
-          // plain FP32 stage only: every root gets up to 5 FP64 Newton steps next,
-          // on its own lane, which costs less than the compensated FP32 stage
-          // run root after root on one thread
-          pok[j] = aberth_mixed_f32<DEG, false>(p, z, P.itmax, true, &its) ? 1 : 0;
-          if (P.dbg) {
-            atomicAdd(&dbg_ref[5], its);
-            atomicAdd(&dbg_ref[6], 1);
+            S.Z[(size_t)slot * DEG + i] =
+                S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
+        }
+        __syncthreads();
+        // The FP32 stage on a lane group per new point, one lane per root,
+        // every root updated from the previous iterate (simultaneous Aberth
+        // steps); the FP32 stopping rule of the reference's iteration.  Up to
+        // 5 FP64 Newton steps per root follow, so the compensated stage is not
+        // needed; a group that does not converge goes to the FP64 fallback.
+        {
+          constexpr int FG = RefGroup<DEG>::G;
+          const int lg = tid & (FG - 1);
+          const unsigned gmask = (FG == 32) ? 0xffffffffu : (((1u << FG) - 1u) << ((tid & 31) - lg));
+          for (int j = tid / FG; j < nsel; j += ES_THREADS / FG) {
+            const int slot = Lcur + j;
+            cf ph[DEG + 1];
+            float alpha[DEG + 1];
+#pragma unroll
+            for (int q = 0; q <= DEG; ++q) {
+              ph[q] = tof(pco[(size_t)j * (DEG + 2) + q]);
+              alpha[q] = cabs(ph[q]) * fmaf(3.8284271247461900976f, (float)q, 1.0f);
+            }
+            cf zr = lg < DEG ? tof(S.Z[(size_t)slot * DEG + lg]) : mkf(0.0f, 0.0f);
+            bool done = lg >= DEG;
+            int it = 0;
+            for (; it < 64; ++it) {
+              cf zall[DEG];
+#pragma unroll
+              for (int q = 0; q < DEG; ++q)
+                zall[q] = mkf(__shfl_sync(gmask, zr.x, q, FG), __shfl_sync(gmask, zr.y, q, FG));
+              if (!done) {
+                const float az = cabs(zr);
+                const bool rev = az > 1.0f;
+                const cf x = rev ? crecip(zr) : zr;
+                cf h, hd;
+                float b;
+                horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+                if (cabs(h) > CGB_EPS32 * b) {
+                  cf sum = mkf(0.0f, 0.0f);
+#pragma unroll
+                  for (int q = 0; q < DEG; ++q)
+                    if (q != lg) sum = sum + crecip(zr - zall[q]);
+                  cf corr;
+                  if (rev) {
+                    const cf z2h = (zr * zr) * h;
+                    const cf d = zr * h;
+                    corr = cdiv(z2h, mkf(d.x * DEG, d.y * DEG) - hd - z2h * sum);
+                  } else {
+                    corr = cdiv(h, hd - h * sum);
+                  }
+                  zr = zr - corr;
+                } else {
+                  done = true;
+                }
+              }
+              if (__all_sync(gmask, done)) break;
+            }
+            const bool ok = __all_sync(gmask, done && isfinite(zr.x) && isfinite(zr.y));
+            if (lg < DEG) S.Z[(size_t)slot * DEG + lg] = tod(zr);
+            if (lg == 0) {
+              pok[j] = ok ? 1 : 0;
+              if (P.dbg) {
+                atomicAdd(&dbg_ref[5], it + 1);
+                atomicAdd(&dbg_ref[6], 1);
+              }
+            }
           }
-#pragma unroll
-          for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
-          pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
-#pragma unroll
-          for (int i = 0; i < DEG; ++i) S.Z[(size_t)slot * DEG + i] = z[i];
         }
         if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
         __syncthreads();
