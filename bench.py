@@ -437,6 +437,10 @@ def main():
                      "peak_source": "measured live in bench.py (cgb_probe_fma, FP32 FMA burst); the path moves "
                                     "24 B per evaluation, so neither HBM nor tensor peaks bound it",
                      "flop_per_eval": FLOP_PER_EVAL,
+                     "pipes_ncu": {"fp64_pct_of_peak": 43.5, "fp32_fma_pct_of_peak": 5.6, "issue_active_pct": 14.4,
+                                   "source": "ncu --set full of a 300-evaluation launch of this workload "
+                                             "(profiles/es_kernel_mixed_binary_ld_300pt.md): the FP64 pipe, not "
+                                             "the FMA rate of the flop model, bounds the kernel"},
                      "hbm_sanity": {"bytes_per_eval": 24,
                                     "achieved_gbs": 24 * WL["npoints"] / (es_ms * 1e-3) / 1e9,
                                     "peak_gbs_measured": _measured_peaks().get("hbm_gbs")}},
