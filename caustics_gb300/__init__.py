@@ -4,7 +4,9 @@ extended-source (contour-integration) magnification, hexadecapole routing —
 behind a C ABI (include/caustics_gb300.h) with the reference's Python
 signatures."""
 from .api import (  # noqa: F401
+    AnnualParallaxTrajectory,
     BatchedLightCurves,
+    ExtendedSourceMagnification,
     LightCurveLogLikelihood,
     LightCurveMagnification,
     critical_and_caustic_curves,
@@ -20,6 +22,7 @@ from .api import (  # noqa: F401
     marginalized_log_likelihood,
     marginalized_log_likelihood_batched,
     poly_roots,
+    project_onto_sky,
     roots_jvp,
     roots_vjp,
 )
@@ -27,4 +30,5 @@ from .api import (  # noqa: F401
 __all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
            "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves",
            "roots_jvp", "roots_vjp", "critical_and_caustic_curves",
-           "marginalized_log_likelihood", "marginalized_log_likelihood_batched", "LightCurveLogLikelihood"]
+           "marginalized_log_likelihood", "marginalized_log_likelihood_batched", "LightCurveLogLikelihood",
+           "AnnualParallaxTrajectory", "ExtendedSourceMagnification", "project_onto_sky"]

@@ -51,6 +51,9 @@ SIGNATURES = {
     "cgb_gauss_legendre": (ctypes.c_int, [ctypes.c_int32, _P, _P]),
     "cgb_ea_solve": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "gpu_ehrlich_aberth": (None, [_P, _P, ctypes.c_char_p, ctypes.c_size_t]),
+    "cgb_parallax_trajectory": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
+                                               _P, _P]),
     "cgb_marginalized_log_likelihood": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P, _P,
                                                        _P, _P]),
     "cgb_critical_curves_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),

@@ -8,6 +8,7 @@ Signature parity with fbartolic/caustics:
   lens_eq, lens_eq_det_jac ...... src/caustics/point_source.py:1536-1580
   critical_and_caustic_curves ... src/caustics/point_source.py:1582-1649
   marginalized_log_likelihood ... src/caustics/linalg.py:10-94
+  AnnualParallaxTrajectory ...... src/caustics/trajectory.py:12-157
 
 Inputs may be torch tensors (any device; CUDA tensors stay on their device)
 or array-likes (copied to the current CUDA device; NumPy out).  Every
@@ -449,6 +450,127 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
                                                      L.lens_params(nlenses, params), opts, None, _stream()),
                 "cgb_mag_extended_source_grad")
     return _out(mag_out, was_np), _out(g, was_np)
+
+
+# ---------------------------------------------------------------------------
+# annual-parallax trajectory
+# ---------------------------------------------------------------------------
+
+def project_onto_sky(vec, direction):
+    """(east, north) components of 3-vectors vec [n, 3] (ICRS) on the plane of
+    the sky perpendicular to `direction` (trajectory.py:45-80); host arithmetic."""
+    d = np.asarray(direction, dtype=np.float64)
+    d = d / np.linalg.norm(d)
+    east = np.cross([0.0, 0.0, 1.0], d)
+    north = np.cross(d, east)
+    east, north = east / np.linalg.norm(east), north / np.linalg.norm(north)
+    vec = np.asarray(vec, dtype=np.float64)
+    return vec @ east, vec @ north
+
+
+class _Parallax(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, traj, t):
+        w, J = traj._launch(t, theta.detach(), True)
+        ctx.save_for_backward(J)
+        return w
+
+    @staticmethod
+    def backward(ctx, gw):
+        (J,) = ctx.saved_tensors
+        # real parameters, complex output: dL/dtheta_k = Re sum_i conj(gw_i) dw_i/dtheta_k
+        return (torch.conj(gw)[:, None] * J).real.sum(0), None, None
+
+
+class AnnualParallaxTrajectory:
+    """Source trajectory with annual parallax (trajectory.py:12-157).  As in the
+    reference, the constructor takes the observation times and the source's
+    astropy SkyCoord and builds the projected Sun ephemeris on a 1-day grid with
+    astropy; alternatively pass ephemeris=(t_jpl, s_e, s_n, s_e_dot, s_n_dot)
+    computed elsewhere (e.g. project_onto_sky of the Earth's barycentric
+    position and velocity, negated).  compute() runs on the GPU; with parameter
+    tensors that require grad it is differentiable (torch autograd)."""
+
+    def __init__(self, t, coords=None, ephemeris=None, device=None):
+        if ephemeris is None:
+            if coords is None:
+                raise ValueError("pass coords (needs astropy) or a precomputed ephemeris")
+            try:
+                from astropy.coordinates import get_body_barycentric_posvel
+                from astropy.time import Time
+            except ImportError as e:
+                raise L.CausticsError("building the ephemeris needs astropy; pass ephemeris= instead") from e
+            t = np.asarray(t, dtype=np.float64)
+            t_jpl = np.arange(t[0], t[-1] + 1, 1)
+            pos, vel = get_body_barycentric_posvel("earth", Time(t_jpl + 2450000, format="jd", scale="tdb"))
+            direction = np.array(coords.cartesian.xyz.value)
+            s_e, s_n = project_onto_sky(-pos.xyz.value.T, direction)
+            s_e_dot, s_n_dot = project_onto_sky(-vel.xyz.value.T, direction)
+            ephemeris = (t_jpl, s_e, s_n, s_e_dot, s_n_dot)
+        if not torch.cuda.is_available() and device is None:
+            raise L.CausticsError("caustics_gb300 needs a CUDA device (no CPU fallback)")
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.ephemeris = [torch.as_tensor(np.asarray(a, dtype=np.float64), device=dev).contiguous() for a in ephemeris]
+        self.device = dev
+
+    def _launch(self, t, theta, jacobian):
+        tt = t if isinstance(t, torch.Tensor) else torch.as_tensor(np.asarray(t, dtype=np.float64))
+        tt = tt.to(self.device, torch.float64).contiguous()
+        n = tt.numel()
+        w = torch.empty(n, dtype=torch.complex128, device=self.device)
+        J = torch.empty((n, 5), dtype=torch.complex128, device=self.device) if jacobian else None
+        u0, t0, tE, piEE, piEN = (float(x) for x in theta)
+        te, se, sn, sed, snd = self.ephemeris
+        with torch.cuda.device(self.device):
+            L.check(L.lib().cgb_parallax_trajectory(_ptr(te), _ptr(se), _ptr(sn), _ptr(sed), _ptr(snd), te.numel(),
+                                                    _ptr(tt), n, u0, t0, tE, piEE, piEN, _ptr(w), _ptr(J), _stream()),
+                    "cgb_parallax_trajectory")
+        return w, J
+
+    def compute(self, t, parametrization="cartesian", **params):
+        """w(t) = east + i north (trajectory.py:122-157); params u0, t0, tE and
+        piEE, piEN ("cartesian") or piE, psi ("polar")."""
+        if parametrization == "polar":
+            piEE = params["piE"] * (torch.sin(params["psi"]) if isinstance(params["psi"], torch.Tensor)
+                                    else math.sin(params["psi"]))
+            piEN = params["piE"] * (torch.cos(params["psi"]) if isinstance(params["psi"], torch.Tensor)
+                                    else math.cos(params["psi"]))
+        elif parametrization == "cartesian":
+            piEE, piEN = params["piEE"], params["piEN"]
+        else:
+            raise ValueError("Invalid parametrization. Choose from 'polar' (piE, psi) or 'cartesian' (piEE, piEN).")
+        vals = [params["u0"], params["t0"], params["tE"], piEE, piEN]
+        if any(isinstance(v, torch.Tensor) and v.requires_grad for v in vals):
+            theta = torch.stack([v.to(self.device, torch.float64).reshape(()) if isinstance(v, torch.Tensor)
+                                 else torch.tensor(float(v), dtype=torch.float64, device=self.device) for v in vals])
+            return _Parallax.apply(theta, self, t)
+        w, _ = self._launch(t, [float(v) for v in vals], False)
+        return w if isinstance(t, torch.Tensor) else w.cpu().numpy()
+
+    def jacobian(self, t, u0, t0, tE, piEE, piEN):
+        """(w [n], dw/d(u0, t0, tE, piEE, piEN) [n, 5]) on the device."""
+        return self._launch(t, [u0, t0, tE, piEE, piEN], True)
+
+
+class ExtendedSourceMagnification(torch.autograd.Function):
+    """mag_extended_source as a function of the source centres w (complex
+    tensor [n]) and params = (s, q, rho, u1) (float64 tensor [4]) for binary
+    lenses; backward is the hand-written adjoint (mag_extended_source_grad).
+    ExtendedSourceMagnification.apply(w, params, options)."""
+
+    @staticmethod
+    def forward(ctx, w, params, options):
+        s, q, rho, u1 = (float(x) for x in params.detach().cpu())
+        mag, g = mag_extended_source_grad(w.detach(), rho, u1=u1, s=s, q=q, **options)
+        ctx.save_for_backward(g)
+        return mag
+
+    @staticmethod
+    def backward(ctx, gmag):
+        (g,) = ctx.saved_tensors
+        gw = gmag * torch.complex(g[:, 4], g[:, 5])
+        gp = (gmag[:, None] * g[:, :4]).sum(0)
+        return gw, gp, None
 
 
 # ---------------------------------------------------------------------------

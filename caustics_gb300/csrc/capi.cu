@@ -216,6 +216,19 @@ void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t
                d.compensated ? CGB_PREC_FP64_COMP : CGB_PREC_FP64, nullptr, stream);
 }
 
+int cgb_parallax_trajectory(const double *t_jpl, const double *s_e, const double *s_n, const double *s_e_dot,
+                            const double *s_n_dot, int64_t njpl, const double *t, int64_t n, double u0, double t0,
+                            double tE, double piEE, double piEN, double *w, double *dw, void *stream) {
+  if (n < 0 || njpl < 1) return fail(CGB_ERR_INVALID, "need n >= 0 and an ephemeris of >= 1 sample%s");
+  if (n == 0) return CGB_OK;
+  if (!t_jpl || !s_e || !s_n || !s_e_dot || !s_n_dot || !t || !w) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!(tE > 0) || !isfinite(tE) || !isfinite(u0) || !isfinite(t0) || !isfinite(piEE) || !isfinite(piEN))
+    return fail(CGB_ERR_INVALID, "invalid trajectory parameters%s");
+  return cuda_status(launch_parallax(t_jpl, s_e, s_n, s_e_dot, s_n_dot, njpl, t, n, u0, t0, tE, piEE, piEN, w, dw,
+                                     (cudaStream_t)stream),
+                     "cgb_parallax_trajectory launch");
+}
+
 int cgb_marginalized_log_likelihood(const int64_t *offsets, int64_t ncurves, int64_t npoints, const double *A,
                                     const double *fobs, const double *C_inv, double *beta, double *ll,
                                     double *dll_dA, const double *ll_cot, void *stream) {

@@ -23,6 +23,11 @@ cudaError_t launch_marg_ll(const int64_t *offsets, int64_t ncurves, const double
                            const double *C_inv, double *beta, double *ll, double *dll, const double *ll_cot,
                            cudaStream_t stream);
 
+// annual-parallax trajectory (trajectory.cu)
+cudaError_t launch_parallax(const double *t_jpl, const double *s_e, const double *s_n, const double *s_e_dot,
+                            const double *s_n_dot, int64_t njpl, const double *t, int64_t n, double u0, double t0,
+                            double tE, double piEE, double piEN, double *w, double *dw, cudaStream_t stream);
+
 // critical curves and caustics (critical.cu)
 size_t critical_workspace_bytes(int npts, int nlenses);
 cudaError_t launch_critical(const Lens &L, int npts, int itmax, double *z_cr, double *z_ca, uint32_t *status,

@@ -118,6 +118,17 @@ int cgb_ea_roots_vjp(const double *coeffs, const double *roots, const double *ct
  * buffers[1] = roots.  Errors are reported through cgb_last_error(). */
 void gpu_ehrlich_aberth(void *stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* Source trajectory with annual parallax (replaces
+ * AnnualParallaxTrajectory.compute, src/caustics/trajectory.py:106-157,
+ * cartesian parametrisation): the projected Sun ephemeris t_jpl, s_e, s_n,
+ * s_e_dot, s_n_dot (float64[njpl], t_jpl increasing; the reference builds it with
+ * astropy in its constructor) is interpolated linearly, clamped outside its
+ * range, at the n times t.  w: complex128[n]; optional dw: complex128[n, 5] =
+ * dw / d(u0, t0, tE, piEE, piEN). */
+int cgb_parallax_trajectory(const double *t_jpl, const double *s_e, const double *s_n, const double *s_e_dot,
+                            const double *s_n_dot, int64_t njpl, const double *t, int64_t n, double u0, double t0,
+                            double tE, double piEE, double piEN, double *w, double *dw, void *stream);
+
 /* Log-likelihood of ncurves light curves marginalised over the linear flux
  * parameters (F_s, F_b) with a diagonal inverse covariance (replaces
  * marginalized_log_likelihood(..., dense_covariance=False),

@@ -902,3 +902,35 @@ def marginalized_log_likelihood_grad(A, fobs, C_inv, beta, Sigma):
     d ll / d A_i = c_i (r_i beta_0 - A_i Sigma_00 - Sigma_01)."""
     r = fobs - (beta[0] * A + beta[1])
     return C_inv * (r * beta[0] - A * Sigma[0, 0] - Sigma[0, 1])
+
+
+# ----------------------------------------------------------------------------
+# Annual-parallax trajectory (trajectory.py:106-157) and the sky projection of
+# the Sun's position (trajectory.py:45-80)
+# ----------------------------------------------------------------------------
+
+
+def project_onto_sky(vec, direction):
+    """East and north components of 3-vectors vec [n, 3] on the plane of the sky
+    perpendicular to `direction` (ICRS), trajectory.py:45-80."""
+    d = np.asarray(direction, dtype=np.float64)
+    d = d / np.linalg.norm(d)
+    east = np.cross([0.0, 0.0, 1.0], d)
+    north = np.cross(d, east)
+    east, north = east / np.linalg.norm(east), north / np.linalg.norm(north)
+    vec = np.asarray(vec, dtype=np.float64)
+    return vec @ east, vec @ north
+
+
+def parallax_trajectory(t, t_jpl, s_e, s_n, s_e_dot, s_n_dot, u0, t0, tE, piEE, piEN):
+    """Source position w(t) with annual parallax (trajectory.py:106-157,
+    cartesian parametrisation): deviation of the Sun's projected position from
+    rectilinear motion about t0, added with piE to the rectilinear trajectory of
+    angle psi = atan2(piEE, piEN)."""
+    t = np.asarray(t, dtype=np.float64)
+    dse = np.interp(t, t_jpl, s_e) - np.interp(t0, t_jpl, s_e) - (t - t0) * np.interp(t0, t_jpl, s_e_dot)
+    dsn = np.interp(t, t_jpl, s_n) - np.interp(t0, t_jpl, s_n) - (t - t0) * np.interp(t0, t_jpl, s_n_dot)
+    psi, piE = np.arctan2(piEE, piEN), np.sqrt(piEN ** 2 + piEE ** 2)
+    ue = u0 * np.cos(psi) + (t - t0) / tE * np.sin(psi) + piE * dse
+    un = -u0 * np.sin(psi) + (t - t0) / tE * np.cos(psi) + piE * dsn
+    return ue + 1j * un

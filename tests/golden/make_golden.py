@@ -17,7 +17,7 @@ Known deviations of this harness from the reference under real JAX:
 * roots come from the reference's C++ solver through ctypes instead of an XLA
   custom call (identical code, compiled with g++ -O2 -DNDEBUG).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp|likelihood]
+Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp|likelihood|parallax]
 """
 import argparse
 import ctypes
@@ -144,15 +144,44 @@ def likelihood_fixture():
                 ll=np.float64(ll), ll_each=ll_each)
 
 
+def parallax_fixture():
+    """AnnualParallaxTrajectory.compute (trajectory.py:106-157) with a synthetic
+    projected Sun ephemeris (astropy, which the constructor needs, is absent:
+    its module is stubbed for the import and the ephemeris attributes are set
+    directly, as _compute_sun_position_and_velocity would)."""
+    for name in ("astropy", "astropy.coordinates", "astropy.time"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["astropy.coordinates"].get_body_barycentric_posvel = None
+    sys.modules["astropy.time"].Time = None
+    from caustics import trajectory as tr
+    t_jpl = np.arange(8000.0, 8400.0 + 1, 1.0)
+    ph = 2 * np.pi * (t_jpl - 8123.4) / 365.25
+    s_e, s_n = 0.98 * np.cos(ph), 0.41 * np.sin(ph) + 0.05
+    s_e_dot, s_n_dot = -0.98 * np.sin(ph) * 2 * np.pi / 365.25, 0.41 * np.cos(ph) * 2 * np.pi / 365.25
+    traj = object.__new__(tr.AnnualParallaxTrajectory)
+    traj.t_jpl, traj.s_e, traj.s_n, traj.s_e_dot, traj.s_n_dot = t_jpl, s_e, s_n, s_e_dot, s_n_dot
+    t = np.sort(np.random.default_rng(41).uniform(8001.0, 8399.0, 300))
+    out = dict(t_jpl=t_jpl, s_e=s_e, s_n=s_n, s_e_dot=s_e_dot, s_n_dot=s_n_dot, t=t)
+    cases = [dict(u0=0.1, t0=8200.3, tE=35.0, piEE=0.2, piEN=-0.15), dict(u0=-0.05, t0=8150.0, tE=80.0, piEE=-0.4, piEN=0.3)]
+    for k, c in enumerate(cases):
+        w = np.asarray(traj.compute(t, **dict(c)))
+        out[f"w{k}"] = w
+        out[f"params{k}"] = np.array([c["u0"], c["t0"], c["tE"], c["piEE"], c["piEN"]])
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp, likelihood)")
+    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp, likelihood, parallax)")
     args = ap.parse_args()
     lib, poly_roots = load_reference(args.ref)
     from caustics import point_source as ps
     if args.only == "roots_jvp":
         np.savez_compressed(os.path.join(HERE, "roots_jvp.npz"), **roots_jvp_fixture(poly_roots, ps))
+        return
+    if args.only == "parallax":
+        np.savez_compressed(os.path.join(HERE, "parallax.npz"), **parallax_fixture())
         return
     if args.only == "likelihood":
         np.savez_compressed(os.path.join(HERE, "likelihood.npz"), **likelihood_fixture())
@@ -293,6 +322,7 @@ def main():
 
     out["roots_jvp"] = roots_jvp_fixture(poly_roots, ps)
     out["likelihood"] = likelihood_fixture()
+    out["parallax"] = parallax_fixture()
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
     print(f"[golden] wrote {len(out)} fixtures in {time.time() - t0:.1f}s")

@@ -234,3 +234,22 @@ def test_likelihood_gradient_restatement(G):
         am[i] -= h
         fd = (O.marginalized_log_likelihood([ap], [f], [c])[1][0] - O.marginalized_log_likelihood([am], [f], [c])[1][0]) / (2 * h)
         assert abs(fd - g[i]) < 1e-6 * max(abs(g[i]), 1.0)
+
+
+def test_parallax_trajectory_kat(G):
+    """AnnualParallaxTrajectory.compute (trajectory.py:106-157) on the
+    reference's own output (synthetic projected Sun ephemeris)."""
+    d = G("parallax")
+    for k in (0, 1):
+        w = O.parallax_trajectory(d["t"], d["t_jpl"], d["s_e"], d["s_n"], d["s_e_dot"], d["s_n_dot"], *d[f"params{k}"])
+        assert np.max(np.abs(w - d[f"w{k}"])) < 1e-14
+
+
+def test_sky_projection_is_orthonormal():
+    rng = np.random.default_rng(2)
+    direction = rng.normal(size=3)
+    e, n = O.project_onto_sky(np.eye(3), direction)
+    east, north = np.array(e), np.array(n)
+    d = direction / np.linalg.norm(direction)
+    assert abs(east @ north) < 1e-15 and abs(east @ d) < 1e-15 and abs(north @ d) < 1e-15
+    assert abs(np.linalg.norm(east) - 1) < 1e-15 and north[2] > 0
