@@ -634,21 +634,43 @@ __device__ __forceinline__ float brightness_bf_fast(float r) {
 //   D_j = conj(zc) - conj(r_j);
 // the FP64 prologue (once per point) provides every difference, so each FP32
 // quantity is small relative to its own scale.
+// Per-evaluation constants of the FP32 quadrature.
+struct LdConst {
+  float c0, u1, irf;
+  float ej[3];  // eps_j / rho
+};
+
 template <int NL>
-__device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, cd zc, cd z0, int j0, int jstep) {
-  const float c0 = (float)(3.0 / (3.0 - It.u1)), u1 = (float)It.u1;
+__device__ __forceinline__ LdConst ld_const(const EsItem &It) {
+  LdConst k;
   const double inv_rho = 1.0 / It.rho;
-  const cf uc = tof((lens_eq<NL>(It.L, zc) - It.w0) * inv_rho);
+  k.c0 = (float)(3.0 / (3.0 - It.u1));
+  k.u1 = (float)It.u1;
+  k.irf = (float)inv_rho;
+#pragma unroll
+  for (int j = 0; j < NL; ++j) k.ej[j] = (float)(It.L.eps[j] * inv_rho);
+  return k;
+}
+
+// th: the limb angle of the contour point's limb point.  zc is an image of
+// w0 + rho e^{i th}, so (lens_eq(zc) - w0) / rho = e^{i th} up to the root's
+// residual (~1e-15), far below the FP32 node arithmetic.
+template <int NL>
+__device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst &K, cd zc, double th, cd z0, int j0,
+                             int jstep) {
+  const float c0 = K.c0, u1 = K.u1;
+  cf uc;
+  sincosf((float)th, &uc.y, &uc.x);
   cf Dj[NL], Dj2[NL];
   float ej[NL];
 #pragma unroll
   for (int j = 0; j < NL; ++j) {
-    cd d = conj(zc) - conj(It.L.r[j]);
+    const cd d = conj(zc) - conj(It.L.r[j]);
     Dj[j] = tof(d);
     Dj2[j] = tof(d * d);
-    ej[j] = (float)(It.L.eps[j] * inv_rho);
+    ej[j] = K.ej[j];
   }
-  const float irf = (float)inv_rho;
+  const float irf = K.irf;
   double acc[2] = {0.0, 0.0};
 #pragma unroll
   for (int isQ = 0; isQ < 2; ++isQ) {
@@ -1442,58 +1464,103 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           tb = t;
         }
         if (P.dbg) __syncthreads();
-        for (int j = tid; j < nsel; j += ES_THREADS) {
-          const int slot = Lcur + j, sl = psl[j];
-          cd *zrow = S.Z + (size_t)slot * DEG;
-          bool ok = pok[j] != 0;
+        // per-point checks and labelling on the same lane groups (lane r: root r
+        // of the new point, row r of its left neighbour)
+        {
+          constexpr int FG = RefGroup<DEG>::G;
+          const int lg = tid & (FG - 1);
+          const unsigned gmask = (FG == 32) ? 0xffffffffu : (((1u << FG) - 1u) << ((tid & 31) - lg));
+          const int gbase = (tid & 31) - lg;
+          const uint32_t all = (1u << DEG) - 1u;
+          for (int j = tid / FG; j < nsel; j += ES_THREADS / FG) {
+            const int slot = Lcur + j, sl = psl[j];
+            cd *zrow = S.Z + (size_t)slot * DEG;
+            const uint32_t f = lg < DEG ? rflag[j * DEG + lg] : 1u;
+            bool ok = pok[j] != 0 && __all_sync(gmask, (f & 1u) != 0);
+            if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
+              double scale = 0.0;
 #pragma unroll
-          for (int i = 0; i < DEG; ++i) ok = ok && (rflag[j * DEG + i] & 1u);
-          if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
-            cd zz[DEG];
-#pragma unroll
-            for (int i = 0; i < DEG; ++i) zz[i] = zrow[i];
-            ok = roots_distinct<DEG>(zz);
-          }
-          uint16_t mkb = 0, pp = 0, zp = 0;
-          if (ok) {
-            for (int i = 0; i < DEG; ++i) {
-              const uint32_t f = rflag[j * DEG + i];
-              mkb |= (uint16_t)(((f >> 1) & 1u) << i);
-              pp |= (uint16_t)(((f >> 2) & 1u) << i);
-              zp |= (uint16_t)(((f >> 3) & 1u) << i);
-              if (f & 16u) flags |= CGB_ST_AMBIGUOUS;
+              for (int q = 0; q < DEG; ++q) scale = fmax(scale, norm2(zrow[q]));
+              bool sep = true;
+              if (lg < DEG)
+                for (int q = lg + 1; q < DEG; ++q)
+                  if (norm2(zrow[lg] - zrow[q]) < 1e-14 * scale) sep = false;
+              ok = __all_sync(gmask, sep);
             }
-          } else {  // the mixed solver's FP64 fallback, then the filter here
-            flags |= CGB_ST_FALLBACK;
-            cd p[DEG + 1], z[DEG], warm[DEG];
+            if (ok) {
+              const uint32_t mkb = (__ballot_sync(gmask, lg < DEG && (f & 2u)) >> gbase) & all;
+              const uint32_t pp = (__ballot_sync(gmask, lg < DEG && (f & 4u)) >> gbase) & all;
+              const uint32_t zp = (__ballot_sync(gmask, lg < DEG && (f & 8u)) >> gbase) & all;
+              if (lg < DEG && (f & 16u)) flags |= CGB_ST_AMBIGUOUS;
+              if (lg == 0) {
+                S.MK[slot] = (uint16_t)mkb;
+                S.PP[slot] = (uint16_t)pp;
+                S.ZP[slot] = (uint16_t)zp;
+              }
+            } else if (lg == 0) {  // the mixed solver's FP64 fallback, then the filter here
+              flags |= CGB_ST_FALLBACK;
+              cd p[DEG + 1], z[DEG], warm[DEG];
 #pragma unroll
-            for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
-            // the FP64 path's own start: the left neighbour's roots plus the jitter
+              for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
+              // the FP64 path's own start: the left neighbour's roots plus the jitter
 #pragma unroll
-            for (int i = 0; i < DEG; ++i)
-              warm[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
-            if (aberth64_fallback<DEG>(p, z, P.itmax, warm) < 0) flags |= CGB_ST_NOCONV;
-            const cd w = pco[(size_t)j * (DEG + 2) + DEG + 1];
+              for (int i = 0; i < DEG; ++i)
+                warm[i] = S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
+              if (aberth64_fallback<DEG>(p, z, P.itmax, warm) < 0) flags |= CGB_ST_NOCONV;
+              const cd w = pco[(size_t)j * (DEG + 2) + DEG + 1];
+              uint16_t mkb = 0, pp = 0, zp = 0;
 #pragma unroll
-            for (int i = 0; i < DEG; ++i) {
-              zrow[i] = z[i];
-              double r, d;
-              lens_filter<NL>(I.L, z[i], w, r, d);
-              if (r < 1e-6) mkb |= 1u << i;
-              if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
-              if (d > 0) pp |= 1u << i;
-              if (d == 0) zp |= 1u << i;
+              for (int i = 0; i < DEG; ++i) {
+                zrow[i] = z[i];
+                double r, d;
+                lens_filter<NL>(I.L, z[i], w, r, d);
+                if (r < 1e-6) mkb |= 1u << i;
+                if (r > 1e-6 / 30 && r < 1e-6 * 30) flags |= CGB_ST_AMBIGUOUS;
+                if (d > 0) pp |= 1u << i;
+                if (d == 0) zp |= 1u << i;
+              }
+              S.MK[slot] = mkb;
+              S.PP[slot] = pp;
+              S.ZP[slot] = zp;
+            }
+            __syncwarp(gmask);
+            // step_map on the group: lane r finds row r's nearest and second
+            // nearest new root; clear when every row's nearest is nearer than
+            // half its second nearest and no two rows share one
+            int best = 0;
+            bool clear = true;
+            if (lg < DEG) {
+              const cd ar = S.Z[(size_t)sl * DEG + lg];
+              double d1 = INFINITY, d2 = INFINITY;
+#pragma unroll
+              for (int q = 0; q < DEG; ++q) {
+                const double d = norm2(zrow[q] - ar);
+                if (d < d1) {
+                  d2 = d1;
+                  d1 = d;
+                  best = q;
+                } else if (d < d2) {
+                  d2 = d;
+                }
+              }
+              clear = d1 < 0.25 * d2;
+            }
+            uint32_t bits = lg < DEG ? (1u << best) : 0u;
+#pragma unroll
+            for (int o = FG >> 1; o > 0; o >>= 1) bits |= __shfl_xor_sync(gmask, bits, o, FG);
+            const bool amb = !__all_sync(gmask, clear) || bits != all;
+            uint64_t m = 0;
+#pragma unroll
+            for (int q = 0; q < DEG; ++q) m = perm_set(m, q, __shfl_sync(gmask, best, q, FG));
+            if (lg == 0) {
+              if (amb && !P.nearest) {  // labelled below by the reference's warm start, on a lane group
+                S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
+              } else {
+                if (amb) m = greedy_match<DEG>(S.Z + (size_t)sl * DEG, zrow);
+                apply_rows<DEG>(zrow, S.MK[slot], S.PP[slot], S.ZP[slot], m);
+              }
             }
           }
-          S.MK[slot] = mkb;
-          S.PP[slot] = pp;
-          S.ZP[slot] = zp;
-          bool amb;
-          const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, zrow, amb);
-          if (amb && !P.nearest)  // labelled below by the reference's warm start, on a lane group
-            S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
-          else
-            apply_rows<DEG>(zrow, S.MK[slot], S.PP[slot], S.ZP[slot], m);
         }
       } else
       for (int k = tid; k < ngap; k += ES_THREADS) {
@@ -1814,6 +1881,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       // groups of G lanes per contour point (G = P.ld_group), each lane taking
       // every G-th node: I_c = sum_i P_i wx_i + Q_i wy_i (trapezoid weights)
       const int G = P.ld_group, groups = ES_THREADS / G, r = tid % G, gid = tid / G;
+      const LdConst ldk = ld_const<NL>(I);
       const int iters = (ntot + groups - 1) / groups;
       int c = 0;
       for (int it = 0; it < iters; ++it) {
@@ -1828,7 +1896,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
           wx = 0.5 * (zn.x - zp.x);
           wy = 0.5 * (zn.y - zp.y);
-          pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, zc, centroid[c], r, G)
+          pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, ldk, zc, S.TH[S.CP[i] / DEG], centroid[c], r, G)
                                : ld_point_fp64<NL>(P, I, zc, centroid[c], r, G);
         }
         for (int o = G >> 1; o > 0; o >>= 1) {
