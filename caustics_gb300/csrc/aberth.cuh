@@ -147,48 +147,6 @@ __device__ int aberth64(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool wa
   return -1;
 }
 
-// Plain FP32 Aberth (the reference's iteration with FP32 epsilon); used where
-// only the labelling of roots is needed (which iterate converges to which root).
-template <int DEG>
-__device__ int aberth32(const cd (&p64)[DEG + 1], cf (&zf)[DEG], int itmax, bool warm, bool real_guess) {
-  cf p[DEG + 1];
-  float alpha[DEG + 1];
-#pragma unroll
-  for (int i = 0; i <= DEG; ++i) {
-    p[i] = tof(p64[i]);
-    alpha[i] = cabs(p[i]);
-  }
-  if (!warm) {
-    cd z[DEG];
-    init_estimates<DEG>(alpha, z, real_guess);
-#pragma unroll
-    for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
-  }
-#pragma unroll
-  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
-  uint32_t conv = 0;
-  const uint32_t all = (1u << DEG) - 1u;
-  for (int it = 0; it < itmax; ++it) {
-#pragma unroll
-    for (int j = 0; j < DEG; ++j) {
-      if (!((conv >> j) & 1u)) {
-        float az = cabs(zf[j]);
-        bool rev = az > 1.0f;
-        cf x = rev ? crecip(zf[j]) : zf[j];
-        cf h, hd;
-        float b;
-        horner_pair<DEG>(p, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
-        if (cabs(h) > CGB_EPS32 * b)
-          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
-        else
-          conv |= 1u << j;
-      }
-    }
-    if (conv == all) return it + 1;
-  }
-  return -1;
-}
-
 // Compensated Horner (error-free transforms) for p and p' at x, optionally with
 // a low-order coefficient part pl (double-float coefficients).  Returns the
 // compensated h, hd and the running error bound eb (horner.h:281-385).

@@ -1,21 +1,29 @@
 // Extended-source magnification by contour integration, one CTA per source
-// position (src/caustics/extended_source.py:56-904, integrate.py:18-121).
+// position, persistent over a list or a device work queue
+// (src/caustics/extended_source.py:56-904, integrate.py:18-121).
 //
 // Phases inside a CTA (256 threads), all state in shared memory:
-//  A  n0 = npts/2 limb points solved in parallel (cold start), rows ordered by
-//     chained greedy matching (extended_source.py:34-53, utils.py:15-40);
+//  A  n0 = npts/2 limb points solved in parallel (cold start, one thread per
+//     point); rows put in the order of the reference's sequential warm-start
+//     chain: clear steps by nearest roots, ambiguous steps and the first point
+//     by the reference's own iteration (refea, bit-exact) on lane groups;
 //  B  10 refinement rounds: gap per interval = max over images |dz| where either
 //     end is a real image, the n_add largest gaps (ties: larger index first, as
-//     argsort(...)[::-1]) get a midpoint solve warm-started from the left
-//     neighbour (extended_source.py:109-135);
-//  C  final chained matching over all limb points: every step's nearest-image
-//     map is computed in parallel; steps whose map is injective compose as
-//     permutations, the rest redo the greedy pass in track order;
-//  D  tracks -> closed tracks / split open segments (extended_source.py:156-309);
+//     argsort(...)[::-1]) get a midpoint point (extended_source.py:109-135),
+//     solved in parallel steps (coefficients per point; FP32 Aberth on a lane
+//     group per point; FP64 Newton and image filter per root; labelling per
+//     point against the left neighbour, the reference's warm start);
+//  C  final chained matching over all limb points (extended_source.py:150-151):
+//     candidate rows sorted by distance in parallel, the greedy pass in integer
+//     arithmetic on one thread;
+//  D  tracks -> closed tracks / split open segments (extended_source.py:156-309),
+//     change points found in parallel;
 //  E  segment linking into <= 3 contours (extended_source.py:312-727);
 //  F  Green's-theorem integral: trapezoid (uniform) or the Dominik (1998) P/Q
 //     line integrals with split Gauss-Legendre quadrature (integrate.py:47-121),
-//     one warp per contour point, FP64 or FP32 (shifted lens equation) nodes.
+//     ld_group lanes per contour point, FP64 or FP32 (shifted lens equation)
+//     nodes;
+//  and with GRAD the hand-written adjoint of A-F (contours recomputed).
 #pragma once
 #include "aberth.cuh"
 #include "aberth_ref.cuh"
@@ -565,10 +573,6 @@ __device__ void merge_segments(EsSmem<DEG> &S, int L) {
 __device__ __forceinline__ double brightness_b(double r) {
   return r <= 1.0 ? 1.0 + sqrt(fmax(1.0 - r * r, 0.0)) : 1.0 - sqrt(fmax(1.0 - 1.0 / (r * r), 0.0));
 }
-__device__ __forceinline__ float brightness_bf(float r) {
-  return r <= 1.0f ? 1.0f + sqrtf(fmaxf(1.0f - r * r, 0.0f)) : 1.0f - sqrtf(fmaxf(1.0f - 1.0f / (r * r), 0.0f));
-}
-
 // split points of integrate.py:49-64
 __device__ __forceinline__ double split_point(double a, double b, double rho) {
   double absd = fabs(b - a);
