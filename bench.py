@@ -261,63 +261,53 @@ def extras_vjp(C, dev, stream, flush):
             "vjp_over_forward_time": vms / fms, "mixed_vs_fp64_grad_median_rel_diff": rel}
 
 
-def extras_triple(C, dev, stream, nsys=1000, per_sys=1000, big=1 << 20):
-    """Triple-lens point source, mixed (FP32 Aberth + compensated double-float
-    Horner + FP64 polish) against FP64: 1000 systems x 1000 positions (seed 1,
-    s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4, 1e-1], psi ~ U[0, 2pi];
-    s = s1, q = q1, q3 = q2, r3 = s2).  Image counts compared per point (the two
-    solvers order roots differently), excluding points whose residual sits within
-    x30 of the reference's 1e-6 image threshold.  Throughput from one
-    2^20-position call on a system the mixed solver handles.""" 
+def extras_triple(C, dev, stream, nsys=1000, big=1 << 20, ncentres=256):
+    """Triple lenses: point-source throughput (FP64 solver; "mixed" routes
+    triple lenses there, its degree-10 FP32 stages being slower than FP64 in a
+    one-polynomial-per-thread kernel) and extended-source throughput, mixed
+    against FP64, on the first six systems whose mass fractions all reach 1e-2
+    (below that the mixed path hands triple lenses to the FP64 solver).
+    Systems: seed 1, s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4,
+    1e-1], psi ~ U[0, 2pi]; s = s1, q = q1, q3 = q2, r3 = s2.  Contour workload
+    per system: 256 source centres ~ U[-1, 1]^2 (seed 7), rho = 1e-2,
+    npts_limb = 300, with and without limb darkening (u1 = 0.5, npts_ld = 100)."""
     import torch
     rng = np.random.default_rng(1)
     sysp = np.stack([rng.uniform(0.5, 2, nsys), rng.uniform(0.5, 2, nsys), 10 ** rng.uniform(-4, 0, nsys),
                      10 ** rng.uniform(-4, -1, nsys), rng.uniform(0, 2 * np.pi, nsys)], axis=1)
-    w = rng.uniform(-1.5, 1.5, (nsys, per_sys)) + 1j * rng.uniform(-1.5, 1.5, (nsys, per_sys))
-    wd = torch.as_tensor(w, device=dev)
-    maxerr, maxerr_clear, mismatch, ambiguous, fallback, root_err = 0.0, 0.0, 0, 0, 0, []
-
-    def popcount(x):
-        x = x.to(torch.int64)
-        return sum(((x >> b) & 1) for b in range(10))
-    for k in range(nsys):
-        p = dict(s=sysp[k, 0], q=sysp[k, 2], q3=sysp[k, 3], r3=sysp[k, 1], psi=sysp[k, 4])
-        m64, z64, k64, s64 = C.mag_point_source(wd[k], nlenses=3, precision="fp64", return_images=True,
-                                                return_status=True, **p)
-        m32, z32, k32, s32 = C.mag_point_source(wd[k], nlenses=3, precision="mixed", return_images=True,
-                                                return_status=True, **p)
-        rel = torch.abs(m32 - m64) / m64
-        amb = ((s64 | s32) & 2) != 0  # residual within x30 of the reference's 1e-6 image threshold
-        maxerr = max(maxerr, float(rel.max().item()))
-        if (~amb).any():
-            maxerr_clear = max(maxerr_clear, float(rel[~amb].max().item()))
-        mismatch += int(((popcount(k32) != popcount(k64)) & ~amb).sum().item())
-        ambiguous += int(amb.sum().item())
-        fallback += int(((s32 & 4) != 0).sum().item())
-        # roots as sets: distance of each FP64 root to the nearest mixed root, relative to max(|z|, 1)
-        d = torch.abs(z64[:, :, None] - z32[:, None, :]).min(dim=2).values / torch.clamp(torch.abs(z64), min=1.0)
-        root_err.append(d.reshape(-1))
-    root_err = torch.cat(root_err)
-    # throughput on the first system whose mass fractions all reach 1e-2 (below
-    # that the mixed path hands triple lenses to the FP64 solver)
     e1 = sysp[:, 2] / (1 + sysp[:, 2] + sysp[:, 3])
     e2 = sysp[:, 2] * e1
-    k0 = int(np.flatnonzero(np.minimum(np.minimum(e1, e2), 1 - e1 - e2) >= 1e-2)[0])
-    p = dict(s=sysp[k0, 0], q=sysp[k0, 2], q3=sysp[k0, 3], r3=sysp[k0, 1], psi=sysp[k0, 4])
-    wb = torch.as_tensor(rng.uniform(-1.5, 1.5, big) + 1j * rng.uniform(-1.5, 1.5, big), device=dev)
-    rate = {}
-    for prec in ("fp64", "mixed"):
-        C.mag_point_source(wb, nlenses=3, precision=prec, **p)
-        rate[prec] = big / (timed(stream, lambda: C.mag_point_source(wb, nlenses=3, precision=prec, **p), 3) * 1e-3)
-    return {"workload": f"1000 systems x 1000 positions, seed 1 (throughput: 2^20 positions of system {k0})",
-            "systems_on_fp64_solver": int((np.minimum(np.minimum(e1, e2), 1 - e1 - e2) < 1e-2).sum()),
-            "fp64_evals_per_s": rate["fp64"], "mixed_evals_per_s": rate["mixed"],
-            "mixed_vs_fp64_max_rel_mag_err": maxerr, "mixed_vs_fp64_max_rel_mag_err_unambiguous": maxerr_clear,
-            "image_count_mismatches_unambiguous": mismatch, "ambiguous_points": ambiguous,
-            "mixed_fp64_fallbacks": fallback,
-            "root_err_vs_fp64": {"median": float(root_err.median().item()),
-                                 "p99": float(torch.quantile(root_err[:1 << 20], 0.99).item()),
-                                 "max": float(root_err.max().item())}}
+    emin = np.minimum(np.minimum(e1, e2), 1 - e1 - e2)
+    systems = np.flatnonzero(emin >= 1e-2)[:6]
+    rng2 = np.random.default_rng(7)
+    ps_rate, es = [], {"ld0": {"fp64": [], "mixed": []}, "ld1": {"fp64": [], "mixed": []}}
+    maxrel, fallbacks = 0.0, 0
+    for k in systems:
+        p = dict(s=sysp[k, 0], q=sysp[k, 2], q3=sysp[k, 3], r3=sysp[k, 1], psi=sysp[k, 4])
+        wb = torch.as_tensor(rng2.uniform(-1.5, 1.5, big) + 1j * rng2.uniform(-1.5, 1.5, big), device=dev)
+        C.mag_point_source(wb, nlenses=3, precision="fp64", **p)
+        ps_rate.append(big / (timed(stream, lambda: C.mag_point_source(wb, nlenses=3, precision="fp64", **p), 3)
+                              * 1e-3))
+        w0 = torch.as_tensor(rng2.uniform(-1, 1, ncentres) + 1j * rng2.uniform(-1, 1, ncentres), device=dev)
+        for ld in (0, 1):
+            res = {}
+            for prec in ("fp64", "mixed"):
+                def f():
+                    return C.mag_extended_source(w0, 1e-2, nlenses=3, npts_limb=300, limb_darkening=bool(ld),
+                                                 u1=0.5, precision=prec, return_status=True, **p)
+                res[prec] = f()
+                es[f"ld{ld}"][prec].append(ncentres / (timed(stream, f, 2) * 1e-3))
+            m64, m32, s32 = res["fp64"][0], res["mixed"][0], res["mixed"][1]
+            maxrel = max(maxrel, float(((m32 - m64).abs() / m64.abs()).max().item()))
+            fallbacks += int(((s32 & 4) != 0).sum().item())
+    gm = lambda v: float(np.exp(np.mean(np.log(v))))
+    return {"workload": f"systems {systems.tolist()} of 1000 (seed 1); point source: 2^20 positions ~ U[-1.5, 1.5]^2 "
+                        "per system; contour: 256 centres, rho 1e-2, npts_limb 300",
+            "systems_on_fp64_solver_of_1000": int((emin < 1e-2).sum()),
+            "point_source_fp64_evals_per_s_geomean": gm(ps_rate),
+            "extended_fp64_evals_per_s_geomean": {"uniform": gm(es["ld0"]["fp64"]), "ld": gm(es["ld1"]["fp64"])},
+            "extended_mixed_evals_per_s_geomean": {"uniform": gm(es["ld0"]["mixed"]), "ld": gm(es["ld1"]["mixed"])},
+            "extended_mixed_vs_fp64_max_rel_err": maxrel, "extended_mixed_fallback_evals": fallbacks}
 
 
 def main():
@@ -508,7 +498,7 @@ def main():
                               "peak_source": "measured live (cgb_probe_fma, FP64 FMA)"},
             "batched_4096_curve_sample": extras_batched(C, dev, stream, flush),
             "vjp_256x1000": extras_vjp(C, dev, stream, flush),
-            "triple_point_source": extras_triple(C, dev, stream),
+            "triple_lens": extras_triple(C, dev, stream),
         })
     if pool is not None:
         rate, n = cpu_rate(pool, cores)

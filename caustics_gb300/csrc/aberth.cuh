@@ -248,12 +248,6 @@ __device__ int aberth64_comp(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bo
   return -1;
 }
 
-// Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
-// polynomial, FP64 Newton polish, FP64 fallback.  Returns the FP32 iteration
-// count, -1 on non-convergence; sets CGB_ST_FALLBACK in flags when used.
-// The FP32 stages of aberth_mixed alone: FP32 Aberth, then the compensated
-// stage against the double-float coefficients.  z returns the FP32 roots;
-// the result says whether every root met the compensated stopping rule.
 // No two roots closer than 1e-7 of the largest root's modulus.  A root set
 // that fails this is not trusted (two starts may have converged onto one root,
 // leaving another root unfound).
@@ -370,6 +364,9 @@ __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
   return false;
 }
 
+// Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
+// polynomial, FP64 Newton polish, FP64 fallback.  Returns the FP32 iteration
+// count, -1 on non-convergence; sets CGB_ST_FALLBACK in flags when used.
 template <int DEG>
 __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
   cf ph[DEG + 1], pl[DEG + 1];

@@ -55,6 +55,18 @@ int solver_precision(const cgb_lens_params &p, int precision) {
   return precision;
 }
 
+// The point-source kernels solve one polynomial per thread.  For degree 10
+// the mixed solver is slower there than FP64 on every triple system measured
+// (2^20 positions each: 5.0-11.3M/s against 16.2-18.2M/s, fallback rates 0 to
+// 28 %): the FP32 and compensated stages run longer than the FP64 iteration
+// they replace.  Triple lenses therefore take the FP64 solver in the
+// point-source kernels; the contour kernel keeps solver_precision's choice
+// (its mixed path measured 1.0-2.9x faster than FP64 on the same systems).
+int point_source_precision(const cgb_lens_params &p, int precision) {
+  if (precision == CGB_PREC_MIXED && p.nlenses == 3) return CGB_PREC_FP64;
+  return precision;
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -267,7 +279,7 @@ int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t 
   if (precision < 0 || precision > 2) return fail(CGB_ERR_INVALID, "unknown precision%s");
   if (itmax < 1) return fail(CGB_ERR_INVALID, "itmax must be >= 1%s");
   return cuda_status(launch_mag_ps(lens_of(lens), w, mag, images, image_mask, n, itmax,
-                                   solver_precision(lens, precision), status,
+                                   point_source_precision(lens, precision), status,
                                    (cudaStream_t)stream),
                      "cgb_mag_point_source launch");
 }
@@ -399,7 +411,7 @@ int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho,
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const int prec = solver_precision(lens, opts->precision);
-  int prec_ps = prec == CGB_PREC_MIXED ? MIXED : FP64;
+  const int prec_ps = point_source_precision(lens, prec) == CGB_PREC_MIXED ? MIXED : FP64;
   rc = cuda_status(launch_lc_points(P.L, lens.q, w, rho, mag, route, n, P.itmax, prec_ps, status, s),
                    "cgb_mag point pass launch");
   if (rc) return rc;

@@ -64,11 +64,14 @@ def test_poly_roots_warm_start(G):
     assert setdist(r, d["roots_plain"][:64]) < 1e-10
 
 
-def test_degree_4_6_10_random():
+@pytest.mark.parametrize("precision", ["fp64", "fp64_comp", "mixed"])
+def test_degree_4_6_10_random(precision):
+    """Every degree and precision of the root-solver kernel (one instantiation
+    per pair) against the oracle's solver."""
     rng = np.random.default_rng(3)
-    for deg in (4, 6, 10):
+    for deg in (4, 5, 6, 10):
         c = rng.normal(size=(200, deg + 1)) + 1j * rng.normal(size=(200, deg + 1))
-        r = C.poly_roots(c)
+        r = C.poly_roots(c, precision=precision)
         ref = O.poly_roots(c, init_mode=0)
         assert setdist(r, ref) < 1e-9
 
