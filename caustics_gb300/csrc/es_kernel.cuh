@@ -619,18 +619,13 @@ __device__ __forceinline__ cf crecip_fast(cf b) {
   const float inv = __fdividef(1.0f, b.x * b.x + b.y * b.y);
   return cf{b.x * inv, -b.y * inv};
 }
-__device__ __forceinline__ float cabs_fast(cf a) {
-  const float n = a.x * a.x + a.y * a.y;
-  return n > 0.0f ? n * rsqrtf(n) : 0.0f;
-}
-__device__ __forceinline__ float brightness_bf_fast(float r) {
-  // B(r) = 1 + sqrt(1 - r^2) inside the limb, 1 - sqrt(1 - 1/r^2) outside
-  if (r <= 1.0f) {
-    const float x = fmaxf(1.0f - r * r, 0.0f);
-    return 1.0f + (x > 0.0f ? x * rsqrtf(x) : 0.0f);
-  }
-  const float x = fmaxf(1.0f - __fdividef(1.0f, r * r), 0.0f);
-  return 1.0f - (x > 0.0f ? x * rsqrtf(x) : 0.0f);
+// B(r) of the brightness profile from n = r^2 with one rsqrt:
+//   r <= 1: 1 + sqrt(1 - n);  r > 1: 1 - sqrt(1 - 1/n) = 1 - a rsqrt(a n), a = n - 1.
+__device__ __forceinline__ float brightness_bn_fast(float n) {
+  const bool inside = n <= 1.0f;
+  const float a = inside ? 1.0f - n : n - 1.0f;
+  const float sq = a > 0.0f ? a * rsqrtf(inside ? a : a * n) : 0.0f;
+  return inside ? 1.0f + sq : 1.0f - sq;
 }
 
 // FP32 nodes on a shifted lens equation:
@@ -659,10 +654,14 @@ __device__ __forceinline__ LdConst ld_const(const EsItem &It) {
 // th: the limb angle of the contour point's limb point.  zc is an image of
 // w0 + rho e^{i th}, so (lens_eq(zc) - w0) / rho = e^{i th} up to the root's
 // residual (~1e-15), far below the FP32 node arithmetic.
+// glf: FP32 copies of the Gauss-Legendre tables in shared memory,
+// [half][0: nodes, 1: weights][j] (the conversions, once per block, are the
+// ones the node loop would otherwise do per node).
 template <int NL>
 __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst &K, cd zc, double th, cd z0, int j0,
-                             int jstep) {
-  const float c0 = K.c0, u1 = K.u1;
+                             int jstep, const float (*glf)[2][GL_MAX]) {
+  // I = c0 (u1 B + 1 - 2 u1) = cu B + cc
+  const float cu = K.c0 * K.u1, cc = K.c0 * (1.0f - 2.0f * K.u1);
   cf uc;
   sincosf((float)th, &uc.y, &uc.x);
   cf Dj[NL], Dj2[NL];
@@ -686,22 +685,38 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst 
       const float lo_r = (float)(lo - b), hi_r = (float)(hi - b);  // relative to the contour point
       const float hw = 0.5f * (hi_r - lo_r), mid = 0.5f * (hi_r + lo_r);
       const int n = half ? P.n2 : P.n1;
-      float sum = 0.0f;
-      for (int j = j0; j < n; j += jstep) {
-        const float d = fmaf(hw, (float)P.gl_x[half][j], mid);
-        // delta = d (Q, along x) or i d (P, along y); conj(delta) = d or -i d
+      // |s|^2 at one node, s = (lens_eq(zc + delta) - w0) / rho; binary lenses
+      // share one reciprocal between the two lens terms
+      auto node_n2 = [&](float d) {
         const cf cdl = isQ ? mkf(d, 0.0f) : mkf(0.0f, -d);
         cf sacc = isQ ? mkf(fmaf(d, irf, uc.x), uc.y) : mkf(uc.x, fmaf(d, irf, uc.y));
+        if constexpr (NL == 2) {
+          const cf den0 = cfma(Dj[0], cdl, Dj2[0]), den1 = cfma(Dj[1], cdl, Dj2[1]);  // D (D + conj(delta))
+          const float n0 = den0.x * den0.x + den0.y * den0.y, n1 = den1.x * den1.x + den1.y * den1.y;
+          const float inv = __fdividef(1.0f, n0 * n1);
+          const float i0 = ej[0] * inv * n1, i1 = ej[1] * inv * n0;
+          const cf t0 = cdl * cf{den0.x * i0, -den0.y * i0}, t1 = cdl * cf{den1.x * i1, -den1.y * i1};
+          sacc = sacc + t0 + t1;
+        } else {
 #pragma unroll
-        for (int k = 0; k < NL; ++k) {
-          const cf den = cfma(Dj[k], cdl, Dj2[k]);  // D (D + conj(delta))
-          const cf t = cdl * crecip_fast(den);
-          sacc = sacc + t * ej[k];
+          for (int k = 0; k < NL; ++k) {
+            const cf den = cfma(Dj[k], cdl, Dj2[k]);  // D (D + conj(delta))
+            sacc = sacc + (cdl * crecip_fast(den)) * ej[k];
+          }
         }
-        const float r = cabs_fast(sacc);
-        const float I = c0 * (u1 * brightness_bf_fast(r) + 1.0f - 2.0f * u1);
-        sum = fmaf((float)P.gl_w[half][j], I, sum);
+        return sacc.x * sacc.x + sacc.y * sacc.y;
+      };
+      // two nodes in flight per lane: independent chains for the in-order pipeline
+      float s0 = 0.0f, s1 = 0.0f;
+      int j = j0;
+      for (; j + jstep < n; j += 2 * jstep) {
+        const float n0 = node_n2(fmaf(hw, glf[half][0][j], mid));
+        const float n1 = node_n2(fmaf(hw, glf[half][0][j + jstep], mid));
+        s0 = fmaf(glf[half][1][j], fmaf(cu, brightness_bn_fast(n0), cc), s0);
+        s1 = fmaf(glf[half][1][j + jstep], fmaf(cu, brightness_bn_fast(n1), cc), s1);
       }
+      if (j < n) s0 = fmaf(glf[half][1][j], fmaf(cu, brightness_bn_fast(node_n2(fmaf(hw, glf[half][0][j], mid))), cc), s0);
+      const float sum = s0 + s1;
       acc[isQ] += (double)hw * (double)sum;
     }
   }
@@ -747,7 +762,8 @@ __device__ __forceinline__ void split_point_grad(double a, double b, double rho,
 }
 
 template <typename R, typename C>
-__device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad &g) {
+__device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad &g,
+                           const float (*glf)[2][GL_MAX]) {
   // shifted lens equation around the contour point (binary: r_0 = a, r_1 = -a)
   const double rho = It.rho, inv_rho = 1.0 / rho;
   const cd uc64 = (lens_eq<2>(It.L, zc) - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
@@ -782,7 +798,14 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
       const int n = half ? P.n2 : P.n1;
       R A = 0, Bl = 0, Bh = 0, Cf = 0, Ck[6] = {0, 0, 0, 0, 0, 0};
       for (int j = 0; j < n; ++j) {
-        const R t = (R)P.gl_x[half][j], w = (R)P.gl_w[half][j];
+        R t, w;
+        if constexpr (sizeof(R) == sizeof(float)) {
+          t = glf[half][0][j];
+          w = glf[half][1][j];
+        } else {
+          t = P.gl_x[half][j];
+          w = P.gl_w[half][j];
+        }
         const R d = hw * t + mid;
         const C cdl = isQ ? C{d, (R)0} : C{(R)0, -d};  // conj(delta)
         // s/rho = uc + delta/rho + sum eps conj(delta) / (D (D + conj(delta))) / rho
@@ -886,7 +909,7 @@ template <int NL, int PREC>
 __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsItem &I, int ncont, int ntot,
                             const int *cstart, const int *cpar, const cd *centroid,
                             double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2], double *pgr,
-                            double *tot_sh, int64_t pi, double *mag) {
+                            double *tot_sh, int64_t pi, double *mag, const float (*glf)[2][GL_MAX]) {
   constexpr int DEG = NL * NL + 1;
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -932,9 +955,9 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
         for (int k = 0; k < 6; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
         PQGrad g;
         if (PREC == MIXED && amp2 <= P.grad_amp2)
-          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g);
+          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g, glf);
         else
-          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g);
+          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g, glf);
         const cd pq = mk(g.P, g.Q);
         atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
         atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
@@ -1061,6 +1084,12 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
   __shared__ double cgr[MAX_CLOSED + N_CONTOURS][2];  // adjoint: dT/dx0_c, dT/dy0_c
   __shared__ double pgr[6];                          // adjoint: direct dT/d(rho, u1, w0x, w0y, a, e1)
   __shared__ double tot_sh;
+  __shared__ float glf[2][2][GL_MAX];  // FP32 Gauss-Legendre tables [half][nodes | weights][j]
+  for (int i = threadIdx.x; i < 2 * GL_MAX; i += ES_THREADS) {
+    const int h = i / GL_MAX, j = i % GL_MAX;
+    glf[h][0][j] = (float)P.gl_x[h][j];
+    glf[h][1][j] = (float)P.gl_w[h][j];
+  }
   const int Lcap = P.Lcap;
   EsSmem<DEG> S;
   {
@@ -1300,7 +1329,10 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           if ((m >> i) & 1u) g2 = fmax(g2, norm2(b[i] - a[i]));
         S.KEY[k] = sqrt(g2);
       }
+      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
+      if (P.dbg && tid == 0) dbg_b[9] += arrival_max() - tb;  // interval lengths alone
+      if (P.dbg) __syncthreads();  // keep the arrival clocks until read
       // rank: larger gap first, ties -> larger index first.  Gaps are >= +0, so
       // their IEEE bit patterns order as integers (integer pipe, not FP64).
       for (int k = tid; k < ngap; k += ES_THREADS) {
@@ -1900,7 +1932,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           cd zp = i > b ? S.Z[S.CP[i - 1]] : zc, zn = i + 1 < e ? S.Z[S.CP[i + 1]] : zc;
           wx = 0.5 * (zn.x - zp.x);
           wy = 0.5 * (zn.y - zp.y);
-          pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, ldk, zc, S.TH[S.CP[i] / DEG], centroid[c], r, G)
+          pq = (PREC == MIXED) ? ld_point_mixed<NL>(P, I, ldk, zc, S.TH[S.CP[i] / DEG], centroid[c], r, G, glf)
                                : ld_point_fp64<NL>(P, I, zc, centroid[c], r, G);
         }
         for (int o = G >> 1; o > 0; o >>= 1) {
@@ -1924,7 +1956,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       }
     }
     __syncthreads();
-    if (GRAD) es_backward<NL, PREC>(P, S, I, ncont, ntot, cstart, cpar, centroid, contour_acc, cgr, pgr, &tot_sh, pi, mag);
+    if (GRAD)
+      es_backward<NL, PREC>(P, S, I, ncont, ntot, cstart, cpar, centroid, contour_acc, cgr, pgr, &tot_sh, pi, mag, glf);
     if (tid == 0 && !GRAD) {
       double tot = 0.0;
       double *dbg = P.dbg ? P.dbg + (size_t)pi * ES_DBG_STRIDE(P.Lcap) : nullptr;

@@ -234,8 +234,9 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
  *  ranking and scan; new-point FP32 stages (FP64: whole solves); FP64 polish
  *  and image filter; per-point labelling; faithful labelling; insertion; then
  *  of the initial sampling: limb solves; first-point labelling and step maps;
- *  chain repair and row permutation; then FP32-stage iterations summed over
- *  the refinement points, and their number]. */
+ *  chain repair and row permutation; then the refinement's interval-length
+ *  computation alone (part of its first sub-phase); then FP32-stage
+ *  iterations summed over the refinement points, and their number]. */
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                               const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
 int64_t cgb_debug_record_len(int32_t npts_limb);
