@@ -174,6 +174,52 @@ static __device__ int block_exclusive_scan(int *buf, int n, int *warp_tot) {
   return carry;
 }
 
+// Length of the limb interval between slots s1 and s2 for the refinement
+// (extended_source.py:110-113): the largest |z2 - z1| over the rows that are a
+// real image at either end, taken as sqrt of the largest squared distance
+// (sqrt is monotone and correctly rounded).
+template <int DEG>
+__device__ __forceinline__ double interval_len(const EsSmem<DEG> &S, int s1, int s2) {
+  const cd *a = S.Z + (size_t)s1 * DEG, *b = S.Z + (size_t)s2 * DEG;
+  const uint16_t m = S.MK[s1] | S.MK[s2];
+  double g2 = 0.0;
+  for (int i = 0; i < DEG; ++i)
+    if ((m >> i) & 1u) g2 = fmax(g2, norm2(b[i] - a[i]));
+  return sqrt(g2);
+}
+
+// Bitonic sort of n (a power of two) pairs (v, ix) into descending order of v,
+// equal v by descending ix; every thread of the block calls it after a block
+// barrier.  Thread t owns compare-exchange t (plus multiples of the block size)
+// of each stage, so at strides up to 32 a warp's exchanges stay inside its own
+// 64-element blocks: two consecutive such stages need only the warp to
+// synchronise, while a stage next to a wider one synchronises the block.
+static __device__ void bitonic_sort_desc(long long *v, uint16_t *ix, int n) {
+  int prev = 0;
+  for (int size = 2; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride > 32 || prev > 32)
+        __syncthreads();
+      else
+        __syncwarp();
+      prev = stride;
+      for (int t = threadIdx.x; t < (n >> 1); t += ES_THREADS) {
+        const int i = 2 * stride * (t / stride) + (t & (stride - 1)), j = i + stride;
+        const long long a = v[i], b = v[j];
+        const uint16_t ia = ix[i], ib = ix[j];
+        const bool b_first = (b > a) || (b == a && ib > ia);  // b precedes a in the final order
+        if (b_first == ((i & size) == 0)) {
+          v[i] = b;
+          v[j] = a;
+          ix[i] = ib;
+          ix[j] = ia;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <int NL, int PREC>
 __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, cd *zrow, const cd *warm,
                                  uint16_t &mkb, uint16_t &pp, uint16_t &zp, uint32_t &flags) {
@@ -1315,45 +1361,48 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     if (P.dbg && tid == 0) clk[1] = clock64();
 
     // ---- B: refinement rounds (extended_source.py:109-135) ----
+    // Storage in the candidate lists' region, unused until the chained
+    // matching: the interval length from each slot to its successor in limb
+    // order (only the intervals next to new points change in a round), the
+    // selected interval of each new point, then either the ranking's sort keys
+    // or the new points' solver scratch.
+    double *GAPS = reinterpret_cast<double *>(S.CAND);  // [Lcap]
+    int *NEWK = reinterpret_cast<int *>(GAPS + Lcap);    // [n_add]
+    unsigned char *rtmp =
+        reinterpret_cast<unsigned char *>(S.CAND) + (((size_t)Lcap * 8 + (size_t)P.n_add * 4 + 15) & ~(size_t)15);
+    for (int k = tid; k + 1 < n0; k += ES_THREADS) GAPS[S.ORD[k]] = interval_len<DEG>(S, S.ORD[k], S.ORD[k + 1]);
     int Lcur = n0;
     long long tb = 0;
     for (int round = 0; round < P.niter; ++round) {
       if (P.dbg && tid == 0 && round == 0) tb = clock64();
       const int ngap = Lcur - 1;
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        const int s1 = S.ORD[k], s2 = S.ORD[k + 1];
-        const cd *a = S.Z + (size_t)s1 * DEG, *b = S.Z + (size_t)s2 * DEG;
-        const uint16_t m = S.MK[s1] | S.MK[s2];
-        double g2 = 0.0;  // max |b - a| = sqrt(max |b - a|^2): sqrt is monotone and correctly rounded
-        for (int i = 0; i < DEG; ++i)
-          if ((m >> i) & 1u) g2 = fmax(g2, norm2(b[i] - a[i]));
-        S.KEY[k] = sqrt(g2);
+      // rank: larger gap first, ties -> larger index first.  Gaps are >= +0, so
+      // their IEEE bit patterns order as integers; padding sorts last.
+      int nsort = 1;
+      while (nsort < ngap) nsort <<= 1;
+      long long *SV = reinterpret_cast<long long *>(rtmp);
+      uint16_t *SI = reinterpret_cast<uint16_t *>(SV + nsort);
+      __syncthreads();  // GAPS of the previous round (or the initial ones) complete
+      for (int k = tid; k < nsort; k += ES_THREADS) {
+        SV[k] = k < ngap ? __double_as_longlong(GAPS[S.ORD[k]]) : -1ll;
+        SI[k] = (uint16_t)(k < ngap ? k : 0);
       }
+      for (int k = tid; k <= ngap; k += ES_THREADS) S.SCAN[k] = 0;
+      if (tid == 0) nlist_sh = 0;
       if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
-      if (P.dbg && tid == 0) dbg_b[9] += arrival_max() - tb;  // interval lengths alone
+      if (P.dbg && tid == 0) dbg_b[9] += arrival_max() - tb;  // key gathering alone
       if (P.dbg) __syncthreads();  // keep the arrival clocks until read
-      // rank: larger gap first, ties -> larger index first.  Gaps are >= +0, so
-      // their IEEE bit patterns order as integers (integer pipe, not FP64).
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        const long long g = __double_as_longlong(S.KEY[k]);
-        int rank = 0;
-        for (int j = 0; j < ngap; ++j) {
-          const long long h = __double_as_longlong(S.KEY[j]);
-          rank += (h > g) || (h == g && j > k);
-        }
-        S.SCAN[k] = rank < P.n_add ? 1 : 0;
-      }
-      if (tid == 0) {
-        S.SCAN[ngap] = 0;
-        nlist_sh = 0;
-      }
+      bitonic_sort_desc(SV, SI, nsort);
+      for (int r = tid; r < P.n_add && r < ngap; r += ES_THREADS) S.SCAN[SI[r]] = 1;
       __syncthreads();
       // positions of the selected gaps -> compact list in SCAN (exclusive scan)
       for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
       __syncthreads();
       if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);  // synchronises the block
+      for (int k = tid; k < ngap; k += ES_THREADS)
+        if (S.KEY[k] != 0.0) NEWK[S.SCAN[k]] = k;
       // each sub-phase ends when its last warp reaches the closing barrier
       auto last_arrival = [&]() {
         long long m = dbg_arr[0];
@@ -1372,9 +1421,9 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         // and image filter of every root in turn, which made these solves the
         // longest path of the refinement; here the FP32 stages run per point,
         // then one lane per (point, root) polishes and filters, then one thread
-        // per point checks the root set and labels it.  Scratch lives in the
-        // candidate lists' storage, unused until the chained matching.
-        cd *pco = reinterpret_cast<cd *>(S.CAND);  // [nsel][DEG + 2]: coefficients, then w
+        // per point checks the root set and labels it.  Scratch lives where the
+        // ranking's sort keys were.
+        cd *pco = reinterpret_cast<cd *>(rtmp);  // [nsel][DEG + 2]: coefficients, then w
         uint32_t *rflag = reinterpret_cast<uint32_t *>(pco + (size_t)nsel * (DEG + 2));  // [nsel][DEG]
         int *pok = reinterpret_cast<int *>(rflag + (size_t)nsel * DEG);                  // [nsel]
         int *psl = pok + nsel;                                                           // [nsel]
@@ -1651,6 +1700,12 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         tb = t;
       }
       if (P.dbg) __syncthreads();  // keep the arrival clocks until read
+      // the intervals on either side of each new point (one thread per point)
+      for (int j = tid; j < nsel; j += ES_THREADS) {
+        const int k = NEWK[j], sl = S.ORD[k], sr = S.ORD[k + 1], m = Lcur + j;
+        GAPS[sl] = interval_len<DEG>(S, sl, m);
+        GAPS[m] = interval_len<DEG>(S, m, sr);
+      }
       // insertion: old position k -> k + (#selected before k); new point after k
       for (int k = tid; k < Lcur; k += ES_THREADS) {
         const int before = S.SCAN[k];
