@@ -1403,6 +1403,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       int nsel = block_exclusive_scan(S.SCAN, ngap + 1, warp_tot);  // synchronises the block
       for (int k = tid; k < ngap; k += ES_THREADS)
         if (S.KEY[k] != 0.0) NEWK[S.SCAN[k]] = k;
+      __syncthreads();
       // each sub-phase ends when its last warp reaches the closing barrier
       auto last_arrival = [&]() {
         long long m = dbg_arr[0];
@@ -1427,9 +1428,10 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         uint32_t *rflag = reinterpret_cast<uint32_t *>(pco + (size_t)nsel * (DEG + 2));  // [nsel][DEG]
         int *pok = reinterpret_cast<int *>(rflag + (size_t)nsel * DEG);                  // [nsel]
         int *psl = pok + nsel;                                                           // [nsel]
-        for (int k = tid; k < ngap; k += ES_THREADS) {
-          if (S.KEY[k] == 0.0) continue;
-          const int j = S.SCAN[k], slot = Lcur + j;
+        // one thread per new point, dense over the first warps: FP64 work
+        // spread over every warp costs each warp the whole instruction stream
+        for (int j = tid; j < nsel; j += ES_THREADS) {
+          const int k = NEWK[j], slot = Lcur + j;
           const int sl = S.ORD[k], sr = S.ORD[k + 1];
           const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
           S.TH[slot] = th;
@@ -1648,24 +1650,22 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           }
         }
       } else
-      for (int k = tid; k < ngap; k += ES_THREADS) {
-        if (S.KEY[k] != 0.0) {
-          const int j = S.SCAN[k];
-          const int slot = Lcur + j;
-          const int sl = S.ORD[k], sr = S.ORD[k + 1];
-          const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
-          S.TH[slot] = th;
-          // warm start from the left neighbour's rows (extended_source.py:79-98,
-          // 128-129); the row order is the reference's warm-start labelling
-          solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
-                                     S.PP[slot], S.ZP[slot], flags);
-          bool amb;
-          const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
-          if (amb && !P.nearest)  // labelled below by the reference's warm start, on a lane group
-            S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
-          else
-            apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
-        }
+      for (int j = tid; j < nsel; j += ES_THREADS) {  // one thread per new point, dense
+        const int k = NEWK[j];
+        const int slot = Lcur + j;
+        const int sl = S.ORD[k], sr = S.ORD[k + 1];
+        const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
+        S.TH[slot] = th;
+        // warm start from the left neighbour's rows (extended_source.py:79-98,
+        // 128-129); the row order is the reference's warm-start labelling
+        solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
+                                   S.PP[slot], S.ZP[slot], flags);
+        bool amb;
+        const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
+        if (amb && !P.nearest)  // labelled below by the reference's warm start, on a lane group
+          S.USED[atomicAdd(&nlist_sh, 1)] = (uint64_t)slot | ((uint64_t)sl << 16);
+        else
+          apply_rows<DEG>(S.Z + (size_t)slot * DEG, S.MK[slot], S.PP[slot], S.ZP[slot], m);
       }
       if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();
