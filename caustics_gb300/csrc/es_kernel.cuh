@@ -361,8 +361,11 @@ __device__ void apply_rows(cd *zrow, uint16_t &mkb, uint16_t &pp, uint16_t &zp, 
 // Chained greedy matching over positions [0, n) of ORD (utils.py:15-40 applied
 // along the limb, extended_source.py:34-53); writes PERM[k] = track -> row.
 // In parallel, every row of position k-1 gets its candidate rows of position k
-// sorted by distance (stable, 4 bits each); the sequential pass is then pure
-// integer work: each track, in track order, takes its first untaken candidate.
+// sorted by distance (stable, 4 bits each).  The sequential pass then runs on
+// one warp, lane t holding track t's row: when the tracks' first candidates
+// are all different, each track takes its own (what the greedy order gives
+// whenever nothing collides); otherwise the tracks pick in track order, each
+// its first untaken candidate.
 template <int DEG>
 __device__ void chain_match(EsSmem<DEG> &S, int n) {
   const int tid = threadIdx.x;
@@ -370,10 +373,10 @@ __device__ void chain_match(EsSmem<DEG> &S, int n) {
     const int k = 1 + idx / DEG, i = idx % DEG;
     const cd a = S.Z[(size_t)S.ORD[k - 1] * DEG + i];
     const cd *b = S.Z + (size_t)S.ORD[k] * DEG;
-    double d[DEG];
+    long long d[DEG];  // squared distances are >= +0: their bit patterns order as integers
     int o[DEG];
     for (int j = 0; j < DEG; ++j) {
-      d[j] = norm2(b[j] - a);
+      d[j] = __double_as_longlong(norm2(b[j] - a));
       o[j] = j;
     }
     for (int j = 1; j < DEG; ++j)  // stable insertion sort
@@ -387,26 +390,42 @@ __device__ void chain_match(EsSmem<DEG> &S, int n) {
     S.CAND[(size_t)k * DEG + i] = packed;
   }
   __syncthreads();
-  if (tid == 0) {
-    uint64_t prev = 0;
-    for (int t = 0; t < DEG; ++t) prev = perm_set(prev, t, t);
-    S.PERM[0] = prev;
+  if (tid < 32) {
+    const unsigned full = 0xffffffffu;
+    const int t = tid;
+    const bool own = t < DEG;
+    int row = t;  // PERM[0] is the identity
+    if (t == 0) {
+      uint64_t ident = 0;
+      for (int q = 0; q < DEG; ++q) ident = perm_set(ident, q, q);
+      S.PERM[0] = ident;
+    }
     for (int k = 1; k < n; ++k) {
-      uint64_t cur = 0;
-      uint32_t taken = 0;
-      for (int t = 0; t < DEG; ++t) {
-        const uint64_t cand = S.CAND[(size_t)k * DEG + perm_get(prev, t)];
-        for (int j = 0; j < DEG; ++j) {
-          const int c = perm_get(cand, j);
-          if (!((taken >> c) & 1u)) {
-            taken |= 1u << c;
-            cur = perm_set(cur, t, c);
-            break;
-          }
+      const uint64_t cand = own ? S.CAND[(size_t)k * DEG + row] : 0ull;
+      const int c0 = (int)(cand & 15u);
+      const unsigned firsts = __reduce_or_sync(full, own ? 1u << c0 : 0u);
+      if (__popc(firsts) == DEG) {
+        row = c0;
+      } else {
+        unsigned taken = 0;
+        for (int tt = 0; tt < DEG; ++tt) {
+          int pick = 0;
+          if (t == tt)
+            for (int j = 0; j < DEG; ++j) {
+              const int c = perm_get(cand, j);
+              if (!((taken >> c) & 1u)) {
+                pick = c;
+                break;
+              }
+            }
+          pick = __shfl_sync(full, pick, tt);
+          taken |= 1u << pick;
+          if (t == tt) row = pick;
         }
       }
-      S.PERM[k] = cur;
-      prev = cur;
+      const uint64_t word = own ? (uint64_t)row << (4 * t) : 0ull;
+      const unsigned lo = __reduce_or_sync(full, (unsigned)word), hi = __reduce_or_sync(full, (unsigned)(word >> 32));
+      if (t == 0) S.PERM[k] = ((uint64_t)hi << 32) | lo;
     }
   }
   __syncthreads();
