@@ -386,47 +386,59 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   const float gam = gamma_const<float>(4 * DEG + 2, CGB_EPS32);
   uint32_t cx = 0, cy = 0;
   const uint32_t all = (1u << DEG) - 1u;
+  // Two loops rather than the reference's one (where a root starts its
+  // compensated steps while others still run plain ones): a warp runs the
+  // costly compensated evaluation only while one of its lanes needs it, and
+  // lanes reach that stage at different iterations.
   int it = 0;
-  for (; it < itmax; ++it) {
+  for (; it < itmax && cx != all; ++it) {
 #pragma unroll
     for (int j = 0; j < DEG; ++j) {
-      float az = cabs(zf[j]);
-      bool rev = az > 1.0f;
-      cf x = rev ? crecip(zf[j]) : zf[j];
-      if (!((cx >> j) & 1u)) {
-        cf h, hd;
-        float b;
-        horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
-        if (cabs(h) > CGB_EPS32 * b)
-          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
+      if ((cx >> j) & 1u) continue;
+      const float az = cabs(zf[j]);
+      const bool rev = az > 1.0f;
+      const cf x = rev ? crecip(zf[j]) : zf[j];
+      cf h, hd;
+      float b;
+      horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+      if (cabs(h) > CGB_EPS32 * b)
+        zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
+      else
+        cx |= 1u << j;
+    }
+  }
+  for (; it < itmax && cy != all; ++it) {
+#pragma unroll
+    for (int j = 0; j < DEG; ++j) {
+      if ((cy >> j) & 1u) continue;
+      const float az = cabs(zf[j]);
+      const bool rev = az > 1.0f;
+      const cf x = rev ? crecip(zf[j]) : zf[j];
+      cf h, hd;
+      float eb;
+      horner_comp<DEG, cf, float>(ph, pl, true, x, rev, h, hd, eb);
+      const float ah = cabs(h);
+      const float bound = CGB_EPS32 * ah + (gam * eb + 2 * CGB_EPS32 * CGB_EPS32 * ah);
+      if (ah > 4 * bound) {
+        const cf c = aberth_corr<DEG>(zf, j, h, hd, rev);
+        if (cabs(c) > 4 * CGB_EPS32 * az)
+          zf[j] = zf[j] - c;
         else
-          cx |= 1u << j;
-      } else if (!((cy >> j) & 1u)) {
-        cf h, hd;
-        float eb;
-        horner_comp<DEG, cf, float>(ph, pl, true, x, rev, h, hd, eb);
-        float ah = cabs(h);
-        float bound = CGB_EPS32 * ah + (gam * eb + 2 * CGB_EPS32 * CGB_EPS32 * ah);
-        if (ah > 4 * bound) {
-          cf c = aberth_corr<DEG>(zf, j, h, hd, rev);
-          if (cabs(c) > 4 * CGB_EPS32 * az)
-            zf[j] = zf[j] - c;
-          else
-            cy |= 1u << j;
-        } else {
           cy |= 1u << j;
-        }
+      } else {
+        cy |= 1u << j;
       }
     }
-    if (cy == all) break;
   }
   bool ok = (cy == all) && isfinite(zf[0].x);
 #pragma unroll
   for (int i = 0; i < DEG; ++i) z[i] = tod(zf[i]);
-  // FP64 Newton polish (forward Horner; degrees are small)
-  double worst = 0.0;
+  // FP64 Newton polish (forward Horner; degrees are small), done when every
+  // correction is at most 2^-40 |z| (compared without a division; a NaN
+  // correction never passes)
+  bool conv = false;
   for (int sweep = 0; sweep < 3 && ok; ++sweep) {
-    worst = 0.0;
+    conv = true;
 #pragma unroll
     for (int j = 0; j < DEG; ++j) {
       cd h = p[DEG], hd = mk(0, 0);
@@ -437,13 +449,11 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
       }
       cd c = cdiv(h, hd);
       z[j] = z[j] - c;
-      double rel = norm2(c) / fmax(norm2(z[j]), 1e-300);
-      worst = fmax(worst, rel);
+      conv = conv && norm2(c) <= 8.271806125530277e-25 * fmax(norm2(z[j]), 1e-300);
     }
-    if (!(worst <= 8.271806125530277e-25)) continue;  // |corr| <= 2^-40 |z|
-    break;
+    if (conv) break;
   }
-  ok = ok && (worst <= 8.271806125530277e-25);
+  ok = ok && conv;
   // distinct roots (Newton alone may merge a near-double pair)
   if (ok) {
     double scale = 0.0;
