@@ -65,6 +65,42 @@ __device__ __forceinline__ void init_estimates(const R (&alpha)[DEG + 1], cd (&z
   for (int i = 0; i < DEG; ++i) z[i] = t[i];
 }
 
+// The same initial estimates in FP32 arithmetic, for the mixed solver whose
+// FP32 iteration starts from them (the FP64 transcendentals would cost several
+// hundred FP64 instructions per polynomial on a part with a narrow FP64 pipe).
+template <int DEG>
+__device__ __forceinline__ void init_estimates_f32(const float (&alpha)[DEG + 1], cf (&z)[DEG]) {
+  int hx[DEG + 1];
+  float hy[DEG + 1];
+  int k = 0;
+  for (int i = DEG; i >= 0; --i) {
+    const float y = alpha[i] > 0.0f ? logf(alpha[i]) : -1e30f;
+    while (k >= 2 &&
+           (float)(hx[k - 1] - hx[k - 2]) * (y - hy[k - 2]) - (hy[k - 1] - hy[k - 2]) * (float)(i - hx[k - 2]) <= 0.0f)
+      --k;
+    hx[k] = i;
+    hy[k] = y;
+    ++k;
+  }
+  cf t[DEG];
+  const float pi2 = 6.28318530717958647693f, th = pi2 / DEG;
+  int n = 0;
+  for (int i = k - 2; i >= 0; --i) {
+    const int nz = hx[i] - hx[i + 1];
+    float r = expf((hy[i + 1] - hy[i]) / (float)nz);
+    if (!(r > 0.0f) || !isfinite(r)) r = 1.0f;
+    const float ang = pi2 / (float)nz;
+    for (int j = 0; j < nz && n + j < DEG; ++j) {
+      float sn, cs;
+      sincosf(ang * (float)j + th * (float)i + 0.7f, &sn, &cs);
+      t[n + j] = mkf(r * cs, r * sn);
+    }
+    n += nz;
+  }
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) z[i] = t[i];
+}
+
 // sum_{i != j} 1 / (z_j - z_i)
 template <int DEG, typename C>
 __device__ __forceinline__ C aberth_sum(const C (&z)[DEG], int j) {
@@ -284,68 +320,6 @@ __device__ int aberth64_fallback(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax
   return (it >= 0 && roots_distinct<DEG>(z)) ? it : -1;
 }
 
-// COMP = false stops after the plain FP32 stage (every root meets the FP32
-// stopping rule), for callers that polish every root in FP64 right after.
-template <int DEG, bool COMP = true>
-__device__ bool aberth_mixed_f32(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, int *iters = nullptr) {
-  cf ph[DEG + 1], pl[DEG + 1];
-  float alpha[DEG + 1];
-#pragma unroll
-  for (int i = 0; i <= DEG; ++i) {
-    ph[i] = tof(p[i]);
-    pl[i] = tof(p[i] - tod(ph[i]));
-    alpha[i] = cabs(ph[i]);
-  }
-  if (!warm) init_estimates<DEG>(alpha, z);
-  cf zf[DEG];
-#pragma unroll
-  for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
-#pragma unroll
-  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
-  const float gam = gamma_const<float>(4 * DEG + 2, CGB_EPS32);
-  uint32_t cx = 0, cy = 0;
-  const uint32_t all = (1u << DEG) - 1u;
-  int it = 0;
-  for (; it < itmax; ++it) {
-#pragma unroll
-    for (int j = 0; j < DEG; ++j) {
-      float az = cabs(zf[j]);
-      bool rev = az > 1.0f;
-      cf x = rev ? crecip(zf[j]) : zf[j];
-      if (!((cx >> j) & 1u)) {
-        cf h, hd;
-        float b;
-        horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
-        if (cabs(h) > CGB_EPS32 * b)
-          zf[j] = zf[j] - aberth_corr<DEG>(zf, j, h, hd, rev);
-        else
-          cx |= 1u << j;
-      } else if (!((cy >> j) & 1u)) {
-        cf h, hd;
-        float eb;
-        horner_comp<DEG, cf, float>(ph, pl, true, x, rev, h, hd, eb);
-        float ah = cabs(h);
-        float bound = CGB_EPS32 * ah + (gam * eb + 2 * CGB_EPS32 * CGB_EPS32 * ah);
-        if (ah > 4 * bound) {
-          cf c = aberth_corr<DEG>(zf, j, h, hd, rev);
-          if (cabs(c) > 4 * CGB_EPS32 * az)
-            zf[j] = zf[j] - c;
-          else
-            cy |= 1u << j;
-        } else {
-          cy |= 1u << j;
-        }
-      }
-    }
-    if (cy == all || (!COMP && cx == all)) break;
-  }
-  const bool ok = (COMP ? cy == all : cx == all) && isfinite(zf[0].x);
-#pragma unroll
-  for (int i = 0; i < DEG; ++i) z[i] = tod(zf[i]);
-  if (iters) *iters = it + 1;
-  return ok;
-}
-
 // FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
 // correction is at most 2^-40 |z|.
 template <int DEG, int SWEEPS = 3>
@@ -377,10 +351,13 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
     pl[i] = tof(p[i] - tod(ph[i]));
     alpha[i] = cabs(ph[i]);
   }
-  if (!warm) init_estimates<DEG>(alpha, z);
   cf zf[DEG];
+  if (warm) {
 #pragma unroll
-  for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
+    for (int i = 0; i < DEG; ++i) zf[i] = tof(z[i]);
+  } else {
+    init_estimates_f32<DEG>(alpha, zf);
+  }
 #pragma unroll
   for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
   const float gam = gamma_const<float>(4 * DEG + 2, CGB_EPS32);
@@ -389,9 +366,15 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   // Two loops rather than the reference's one (where a root starts its
   // compensated steps while others still run plain ones): a warp runs the
   // costly compensated evaluation only while one of its lanes needs it, and
-  // lanes reach that stage at different iterations.
+  // lanes reach that stage at different iterations.  The FP32 stopping rule
+  // sits at FP32's own Horner rounding level, so a converged root can keep
+  // missing it: the FP32 stage stops after 128 iterations and such roots go on
+  // to the compensated stage (at most 64 iterations), whose double-float
+  // evaluation can meet its bound.  Whatever still fails takes the FP64
+  // fallback below.
   int it = 0;
-  for (; it < itmax && cx != all; ++it) {
+  const int it32 = min(itmax, 128);
+  for (; it < it32 && cx != all; ++it) {
 #pragma unroll
     for (int j = 0; j < DEG; ++j) {
       if ((cx >> j) & 1u) continue;
@@ -407,7 +390,8 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
         cx |= 1u << j;
     }
   }
-  for (; it < itmax && cy != all; ++it) {
+  const int itc = min(itmax, it + 64);
+  for (; it < itc && cy != all; ++it) {
 #pragma unroll
     for (int j = 0; j < DEG; ++j) {
       if ((cy >> j) & 1u) continue;
