@@ -314,15 +314,20 @@ int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, in
                      "cgb_mag_extended_source_grad launch");
 }
 
+// Workspace of the batched entry points: a 16-byte queue header, one queue
+// slot per point, then one first-limb-point row order per point.  Only the
+// first two are required: with a workspace of 16 + 8 npoints bytes the contour
+// kernel orders each first limb point itself (one lane group per block, slower).
 size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints) {
-  return 16 + 8 * (size_t)(npoints > 0 ? npoints : 0);
+  return 16 + 16 * (size_t)(npoints > 0 ? npoints : 0);
 }
+static size_t batched_queue_bytes(int64_t npoints) { return 16 + 8 * (size_t)(npoints > 0 ? npoints : 0); }
 
 static int batched_setup(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
                          int64_t npoints, const cgb_es_options *opts, void *ws, size_t ws_bytes, EsParams &P) {
   if (ncurves < 1 || npoints < 0) return fail(CGB_ERR_INVALID, "need ncurves >= 1 and npoints >= 0%s");
   if (!offsets || !curves || (npoints > 0 && !t)) return fail(CGB_ERR_INVALID, "null buffer%s");
-  if (!ws || ws_bytes < cgb_mag_lc_batched_workspace_bytes(npoints))
+  if (!ws || ws_bytes < batched_queue_bytes(npoints))
     return fail(CGB_ERR_INVALID, "workspace too small (see cgb_mag_lc_batched_workspace_bytes)%s");
   cgb_lens_params dummy{2, 1.0, 1.0, 0.0, 0.0, 0.0};
   int rc = make_es_params(dummy, 1.0, opts, P);
@@ -334,6 +339,8 @@ static int batched_setup(const int64_t *offsets, const double *t, const cgb_curv
   P.qcount = reinterpret_cast<const int64_t *>(ws);
   P.qhead = reinterpret_cast<unsigned long long *>((char *)ws + 8);
   P.qlist = reinterpret_cast<const int64_t *>((char *)ws + 16);
+  if (ws_bytes >= cgb_mag_lc_batched_workspace_bytes(npoints))
+    P.perm0 = reinterpret_cast<const uint64_t *>((char *)ws + batched_queue_bytes(npoints));
   P.qchunk = opts->queue_chunk > 0 ? opts->queue_chunk : 1;
   return CGB_OK;
 }
@@ -427,7 +434,8 @@ int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho,
 // buffer assignment (the reference's GPU kernel called cudaMalloc per call
 // instead, lib/ehrlich_aberth/kernels.cc.cu:72-76), and a plain C caller that
 // binds only this ABI may run where no allocator is at hand.  For them the
-// queue header and queue slots live in a fixed, file-scope device array.
+// queue header and queue slots live in a fixed, file-scope device array (and
+// the first-point row orders too, for calls of at most 131,072 points).
 namespace {
 constexpr int64_t kNoAllocMaxPoints = 1 << 18;  // 262,144 light-curve points per call
 constexpr size_t kNoAllocScratchBytes = 16 + 8 * (size_t)kNoAllocMaxPoints;  // 2 MiB + 16 B per device

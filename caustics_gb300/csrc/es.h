@@ -50,6 +50,10 @@ struct EsParams {
   int ld_group;               // lanes sharing one contour point's quadrature nodes (1, 2, 4, 8)
   double grad_amp2;           // mixed adjoint: FP64 quadrature where max |dz/dtheta|^2 exceeds this
   int nearest;                // 1: nearest-root row labelling (no faithful solves)
+  // row order of each item's first limb point, filled by es_first_order_kernel
+  // ahead of the contour kernel (indexed by item ordinal); null: the contour
+  // kernel orders it itself
+  const uint64_t *perm0;
   // adjoint (GRAD kernels): per-point gradient rows [n][6] of
   // (s, q, rho, u1, Re w, Im w), or for batched light curves the cotangent
   // weighted sum per curve [ncurves][8] of (s, q, rho, u1, u0, alpha, t0, tE)

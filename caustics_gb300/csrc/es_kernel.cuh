@@ -1123,6 +1123,89 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
   }
 }
 
+// Source, lens and limb-darkening parameters of point pi: a batched light
+// curve's point (curve by bisection of offsets, rectilinear trajectory), or a
+// source centre of a single lens.
+__device__ __forceinline__ EsItem make_item(const EsParams &P, const cd *w0s, int64_t pi) {
+  EsItem it;
+  if (P.curves) {
+    int64_t lo = 0, hi = P.ncurves - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (P.offsets[mid] <= pi) lo = mid; else hi = mid - 1;
+    }
+    const CurveDev cv = P.curves[lo];
+    it.L = make_lens(2, cv.s, cv.q, 0.0, 0.0, 0.0);
+    it.rho = cv.rho;
+    it.u1 = P.ld ? cv.u1 : 0.0;
+    const double tau = (P.times[pi] - cv.t0) / cv.tE;
+    double sa, ca;
+    sincos(cv.alpha, &sa, &ca);
+    it.w0 = mk(cv.u0 * ca + tau * sa + it.L.x_cm, -cv.u0 * sa + tau * ca);
+    it.s = cv.s;
+    it.q = cv.q;
+    it.curve = lo;
+    it.tau = tau;
+  } else {
+    it.L = P.L;
+    it.rho = P.rho;
+    it.u1 = P.u1;
+    const cd w = w0s[pi];
+    it.w0 = mk(w.x + P.L.x_cm, w.y);
+    it.s = P.s_user;
+    it.q = P.q_user;
+    it.curve = -1;
+    it.tau = 0.0;
+  }
+  return it;
+}
+
+// Limb angle of initial point k: jnp.linspace(-pi, pi, n0 - 1, endpoint=False)
+// then pi - 1e-8, rounded as NumPy does.
+__device__ __forceinline__ double limb_theta(int k, int n0) {
+  const double step = 6.283185307179586 / (double)(n0 - 1);
+  return (k < n0 - 1) ? __dadd_rn(__dmul_rn((double)k, step), -3.141592653589793) : 3.141592653589793 - 1e-8;
+}
+
+// Row order of the first limb point for every item of a launch, ahead of the
+// contour kernel (which then reads perm0[item] instead of solving): one lane
+// group per item, several items per warp, so each FP64 instruction of the
+// reference's cold-start iteration serves several items.  Lane 0 of a group
+// first repeats the contour kernel's fast solve of that point (same polynomial,
+// same deterministic solver), whose roots are the raw rows to order.
+// Items are enumerated exactly as the contour kernel takes them.
+constexpr int FO_THREADS = 128;
+template <int NL, int PREC>
+__global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsParams P, const cd *__restrict__ w0s,
+                                                                   const int64_t *__restrict__ index,
+                                                                   const uint8_t *__restrict__ route,
+                                                                   int64_t npoints, uint64_t *__restrict__ perm0) {
+  constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G, NG = FO_THREADS / G;
+  __shared__ cd zs[NG][DEG];
+  const int g = threadIdx.x / G, r = threadIdx.x & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) - r));
+  const int64_t nitems = P.qhead ? *P.qcount : npoints;
+  for (int64_t it = (int64_t)blockIdx.x * NG + g; it < nitems; it += (int64_t)gridDim.x * NG) {
+    const int64_t pi = P.qhead ? P.qlist[it] : (index ? index[it] : it);
+    if (route && route[pi] == 0) continue;  // uniform over the group
+    const EsItem I = make_item(P, w0s, pi);
+    const double th = limb_theta(0, P.n0);
+    if (r == 0) {
+      cd z[DEG];
+      uint16_t mkb, pp, zp;
+      uint32_t flags = 0;
+      solve_limb_point<NL, PREC>(P, I, th, z, nullptr, mkb, pp, zp, flags);
+#pragma unroll
+      for (int i = 0; i < DEG; ++i) zs[g][i] = z[i];
+    }
+    __syncwarp(gmask);
+    int its;
+    const uint64_t o = first_point_order_group<NL>(P, I, th, zs[g], its);
+    if (r == 0) perm0[it] = o;
+    __syncwarp(gmask);
+  }
+}
+
 template <int NL, int PREC, bool GRAD = false>
 __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                         const int64_t *__restrict__ index,
@@ -1144,7 +1227,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
                                            // whole solves, polish + filter, per-point labelling, faithful, insertion)
   __shared__ long long dbg_arr[ES_WARPS];  // diagnostics: each warp's clock on reaching a barrier
   __shared__ long long clk[8];
-  __shared__ int64_t item_sh;
+  __shared__ int64_t item_sh, iord_sh;  // point index, item ordinal
   __shared__ EsItem item;
   __shared__ double cgr[MAX_CLOSED + N_CONTOURS][2];  // adjoint: dT/dx0_c, dT/dy0_c
   __shared__ double pgr[6];                          // adjoint: direct dT/d(rho, u1, w0x, w0y, a, e1)
@@ -1213,10 +1296,12 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         }
         it = chunk_next++;
         item_sh = it < *P.qcount ? P.qlist[it] : -1;
+        iord_sh = it;
       } else {
         it = static_next;
         static_next += gridDim.x;
         item_sh = it < npoints ? (index ? index[it] : it) : -1;
+        iord_sh = it;
       }
     }
     __syncthreads();
@@ -1227,36 +1312,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       continue;
     }
     if (tid == 0) {
-      if (P.curves) {
-        // batched light curves: curve of point pi by bisection of offsets
-        int64_t lo = 0, hi = P.ncurves - 1;
-        while (lo < hi) {
-          int64_t mid = (lo + hi + 1) >> 1;
-          if (P.offsets[mid] <= pi) lo = mid; else hi = mid - 1;
-        }
-        const CurveDev cv = P.curves[lo];
-        item.L = make_lens(2, cv.s, cv.q, 0.0, 0.0, 0.0);
-        item.rho = cv.rho;
-        item.u1 = P.ld ? cv.u1 : 0.0;
-        const double tau = (P.times[pi] - cv.t0) / cv.tE;
-        double sa, ca;
-        sincos(cv.alpha, &sa, &ca);
-        item.w0 = mk(cv.u0 * ca + tau * sa + item.L.x_cm, -cv.u0 * sa + tau * ca);
-        item.s = cv.s;
-        item.q = cv.q;
-        item.curve = lo;
-        item.tau = tau;
-      } else {
-        item.L = P.L;
-        item.rho = P.rho;
-        item.u1 = P.u1;
-        cd w = w0s[pi];
-        item.w0 = mk(w.x + P.L.x_cm, w.y);
-        item.s = P.s_user;
-        item.q = P.q_user;
-        item.curve = -1;
-        item.tau = 0.0;
-      }
+      item = make_item(P, w0s, pi);
       sflags = 0;
     }
     uint32_t flags = 0;
@@ -1271,10 +1327,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     // ---- A: initial limb sampling (extended_source.py:100-107) ----
     const int n0 = P.n0;
     for (int k = tid; k < n0; k += ES_THREADS) {
-      // jnp.linspace(-pi, pi, n0 - 1, endpoint=False) then pi - 1e-8, rounded as NumPy does
-      const double step = 6.283185307179586 / (double)(n0 - 1);
-      double th = (k < n0 - 1) ? __dadd_rn(__dmul_rn((double)k, step), -3.141592653589793)
-                               : 3.141592653589793 - 1e-8;
+      const double th = limb_theta(k, n0);
       S.TH[k] = th;
       S.ORD[k] = (uint16_t)k;
       solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)k * DEG, nullptr, S.MK[k], S.PP[k], S.ZP[k], flags);
@@ -1303,6 +1356,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         for (int t = 0; t < DEG; ++t) ident = perm_set(ident, t, t);
         S.PERM[0] = ident;
       }
+    } else if (P.perm0) {  // ordered ahead of this kernel (es_first_order_kernel)
+      if (tid == 0) S.PERM[0] = P.perm0[iord_sh];
     } else if (tid < RG) {
       int its;
       const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z, its);
@@ -2084,6 +2139,15 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, ES_THREADS, smem);
     grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  if (P.perm0 && !P.nearest) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    es_first_order_kernel<NL, PREC><<<sms * 8, FO_THREADS, 0, stream>>>(P, w0, index, route, n,
+                                                                         const_cast<uint64_t *>(P.perm0));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
   k<<<grid, ES_THREADS, smem, stream>>>(P, w0, index, route, n, mag, status);
   return cudaGetLastError();

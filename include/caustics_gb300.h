@@ -186,8 +186,11 @@ int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, in
 int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
             const cgb_es_options *opts, uint32_t *status, void *stream);
 
-/* Workspace (device bytes) the batched entry points need for npoints points:
- * a work-queue header and one queue slot per point. */
+/* Workspace (device bytes) the batched entry points use for npoints points:
+ * a 16-byte work-queue header, one 8-byte queue slot per point, then one
+ * 8-byte first-limb-point row order per point (16 + 16 npoints).  A workspace
+ * of only 16 + 8 npoints bytes is accepted too: the contour kernel then orders
+ * each first limb point itself, which is slower. */
 size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints);
 
 /* mag() of ncurves binary-lens light curves of uneven lengths in one pass:

@@ -56,6 +56,22 @@ def test_batched_matches_single_curve_calls(precision):
         assert np.max(np.abs(m[sl] - ref) / ref) < (1e-12 if precision == "fp64" else 1e-10)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_first_point_order_kernel_matches_in_kernel_order(precision):
+    """With a full workspace (16 + 16 n bytes) every first limb point is
+    ordered by a kernel of its own ahead of the contour kernel; with the queue
+    alone (16 + 8 n bytes) the contour kernel orders it itself.  The two give
+    the same magnifications bit for bit."""
+    off, t, cv = draw_curves(8, seed=21)
+    n = len(t)
+    full = C.mag_lc_batched(off, t, cv, precision=precision, **OPTS).cpu().numpy()
+    dev = torch.device("cuda")
+    out = (torch.empty(n, dtype=torch.float64, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+           torch.zeros(n, dtype=torch.int32, device=dev), torch.empty(16 + 8 * n, dtype=torch.uint8, device=dev))
+    small = C.mag_lc_batched(off, t, cv, precision=precision, out=out, **OPTS).cpu().numpy()
+    assert np.array_equal(full, small)
+
+
 def test_batched_vs_oracle():
     off, t, cv = draw_curves(4, seed=5, nmin=6, nmax=10)
     m = C.mag_lc_batched(off, t, cv, precision="mixed", **OPTS).cpu().numpy()
