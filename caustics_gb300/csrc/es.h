@@ -69,7 +69,7 @@ struct EsParams {
 // clock64 at the end of phases A..F (6) and the start (1) + 1 spare, theta[0..L)]
 #define ES_DBG_CLK (3 + 4 * 13)
 #define ES_DBG_HEAD (ES_DBG_CLK + 8)
-#define ES_DBG_SUB 10  // refinement and initial-sampling sub-phase clocks
+#define ES_DBG_SUB 9  // refinement and initial-sampling sub-phase clocks
 #define ES_DBG_STRIDE(lcap) (ES_DBG_HEAD + (lcap) + ES_DBG_SUB + 2)  // ... stored after theta, then 2 counters
 
 size_t es_smem_bytes(const EsParams &P, int nl, bool grad = false);

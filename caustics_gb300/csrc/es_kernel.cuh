@@ -1435,40 +1435,47 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     if (P.dbg && tid == 0) clk[1] = clock64();
 
     // ---- B: refinement rounds (extended_source.py:109-135) ----
-    // Storage in the candidate lists' region, unused until the chained
-    // matching: the interval length from each slot to its successor in limb
-    // order (only the intervals next to new points change in a round), the
-    // selected interval of each new point, then either the ranking's sort keys
-    // or the new points' solver scratch.
-    double *GAPS = reinterpret_cast<double *>(S.CAND);  // [Lcap]
-    int *NEWK = reinterpret_cast<int *>(GAPS + Lcap);    // [n_add]
-    unsigned char *rtmp =
-        reinterpret_cast<unsigned char *>(S.CAND) + (((size_t)Lcap * 8 + (size_t)P.n_add * 4 + 15) & ~(size_t)15);
-    for (int k = tid; k + 1 < n0; k += ES_THREADS) GAPS[S.ORD[k]] = interval_len<DEG>(S, S.ORD[k], S.ORD[k + 1]);
+    // The intervals are ranked (larger length first, ties: larger limb position
+    // first) once, by a sort of the initial ones; a round then takes the head of
+    // that list, and only the intervals next to its new points are sorted and
+    // merged into the rest, whose order a round does not change (their
+    // positions shift by the number of new points before them).  Lengths are
+    // >= +0, so their IEEE bit patterns order as integers.  Storage in the
+    // candidate lists' region, unused until the chained matching: the ranked
+    // list (length bits, limb position), the selected interval of each new
+    // point, then scratch: the initial sort's keys, the new points' solver
+    // scratch, or the new intervals and the merged list.
+    long long *SLV = reinterpret_cast<long long *>(S.CAND);                      // [Lcap]
+    uint16_t *SLP = reinterpret_cast<uint16_t *>(SLV + Lcap);                     // [Lcap]
+    int *NEWK = reinterpret_cast<int *>(S.CAND) + ((size_t)Lcap * 10 + 3) / 4;   // [n_add]
+    unsigned char *rtmp = reinterpret_cast<unsigned char *>(S.CAND) +
+                          (((size_t)Lcap * 10 + 4 + (size_t)P.n_add * 4 + 15) & ~(size_t)15);
+    {
+      const int m0 = n0 - 1;
+      int nsort = 1;
+      while (nsort < m0) nsort <<= 1;
+      long long *SV = reinterpret_cast<long long *>(rtmp);
+      uint16_t *SI = reinterpret_cast<uint16_t *>(SV + nsort);
+      for (int k = tid; k < nsort; k += ES_THREADS) {
+        SV[k] = k < m0 ? __double_as_longlong(interval_len<DEG>(S, S.ORD[k], S.ORD[k + 1])) : -1ll;
+        SI[k] = (uint16_t)(k < m0 ? k : 0);
+      }
+      __syncthreads();
+      bitonic_sort_desc(SV, SI, nsort);
+      for (int k = tid; k < m0; k += ES_THREADS) {
+        SLV[k] = SV[k];
+        SLP[k] = SI[k];
+      }
+    }
     int Lcur = n0;
     long long tb = 0;
     for (int round = 0; round < P.niter; ++round) {
       if (P.dbg && tid == 0 && round == 0) tb = clock64();
       const int ngap = Lcur - 1;
-      // rank: larger gap first, ties -> larger index first.  Gaps are >= +0, so
-      // their IEEE bit patterns order as integers; padding sorts last.
-      int nsort = 1;
-      while (nsort < ngap) nsort <<= 1;
-      long long *SV = reinterpret_cast<long long *>(rtmp);
-      uint16_t *SI = reinterpret_cast<uint16_t *>(SV + nsort);
-      __syncthreads();  // GAPS of the previous round (or the initial ones) complete
-      for (int k = tid; k < nsort; k += ES_THREADS) {
-        SV[k] = k < ngap ? __double_as_longlong(GAPS[S.ORD[k]]) : -1ll;
-        SI[k] = (uint16_t)(k < ngap ? k : 0);
-      }
       for (int k = tid; k <= ngap; k += ES_THREADS) S.SCAN[k] = 0;
       if (tid == 0) nlist_sh = 0;
-      if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
-      __syncthreads();
-      if (P.dbg && tid == 0) dbg_b[9] += arrival_max() - tb;  // key gathering alone
-      if (P.dbg) __syncthreads();  // keep the arrival clocks until read
-      bitonic_sort_desc(SV, SI, nsort);
-      for (int r = tid; r < P.n_add && r < ngap; r += ES_THREADS) S.SCAN[SI[r]] = 1;
+      __syncthreads();  // the ranked list of the previous round complete
+      for (int r = tid; r < P.n_add && r < ngap; r += ES_THREADS) S.SCAN[SLP[r]] = 1;
       __syncthreads();
       // positions of the selected gaps -> compact list in SCAN (exclusive scan)
       for (int k = tid; k <= ngap; k += ES_THREADS) S.KEY[k] = (double)S.SCAN[k];  // keep flags
@@ -1774,12 +1781,29 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         tb = t;
       }
       if (P.dbg) __syncthreads();  // keep the arrival clocks until read
-      // the intervals on either side of each new point (one thread per point)
-      for (int j = tid; j < nsel; j += ES_THREADS) {
-        const int k = NEWK[j], sl = S.ORD[k], sr = S.ORD[k + 1], m = Lcur + j;
-        GAPS[sl] = interval_len<DEG>(S, sl, m);
-        GAPS[m] = interval_len<DEG>(S, m, sr);
+      // the intervals on either side of each new point (one thread per point),
+      // at their limb positions after the insertion; the rest of the ranked
+      // list keeps its order, its positions shift past the new points
+      const int nb = 2 * nsel;
+      int nbs = 1;
+      while (nbs < nb) nbs <<= 1;
+      long long *NBV = reinterpret_cast<long long *>(rtmp);  // [nbs] new intervals
+      uint16_t *NBP = reinterpret_cast<uint16_t *>(NBV + nbs);
+      long long *MGV = reinterpret_cast<long long *>(rtmp + (((size_t)nbs * 10 + 15) & ~(size_t)15));  // merged
+      uint16_t *MGP = reinterpret_cast<uint16_t *>(MGV + (ngap + nsel));
+      for (int j = tid; j < nbs; j += ES_THREADS) {
+        if (j < nsel) {
+          const int k = NEWK[j], sl = S.ORD[k], sr = S.ORD[k + 1], m = Lcur + j;
+          NBV[2 * j] = __double_as_longlong(interval_len<DEG>(S, sl, m));
+          NBP[2 * j] = (uint16_t)(k + j);
+          NBV[2 * j + 1] = __double_as_longlong(interval_len<DEG>(S, m, sr));
+          NBP[2 * j + 1] = (uint16_t)(k + j + 1);
+        } else if (j >= nb) {
+          NBV[j] = -1ll;
+          NBP[j] = 0;
+        }
       }
+      for (int r = nsel + tid; r < ngap; r += ES_THREADS) SLP[r] = (uint16_t)(SLP[r] + S.SCAN[SLP[r]]);
       // insertion: old position k -> k + (#selected before k); new point after k
       for (int k = tid; k < Lcur; k += ES_THREADS) {
         const int before = S.SCAN[k];
@@ -1788,6 +1812,35 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       }
       __syncthreads();
       for (int k = tid; k < Lcur + nsel; k += ES_THREADS) S.ORD[k] = S.ORD2[k];
+      bitonic_sort_desc(NBV, NBP, nbs);  // starts after the barrier above, ends with one
+      {
+        // merge the rest of the ranked list (ma entries) with the new intervals
+        // (nb): each entry's place = its own index + the entries of the other
+        // list ranked before it (keys are distinct: positions are)
+        const long long *AV = SLV + nsel;
+        const uint16_t *AP = SLP + nsel;
+        const int ma = ngap - nsel;
+        for (int i = tid; i < ma + nb; i += ES_THREADS) {
+          const bool fromA = i < ma;
+          const long long v = fromA ? AV[i] : NBV[i - ma];
+          const int pos = fromA ? AP[i] : NBP[i - ma];
+          const long long *OV = fromA ? NBV : AV;
+          const uint16_t *OP = fromA ? NBP : AP;
+          int lo = 0, hi = fromA ? nb : ma;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (OV[mid] > v || (OV[mid] == v && OP[mid] > pos)) lo = mid + 1; else hi = mid;
+          }
+          const int at = (fromA ? i : i - ma) + lo;
+          MGV[at] = v;
+          MGP[at] = (uint16_t)pos;
+        }
+        __syncthreads();
+        for (int i = tid; i < ma + nb; i += ES_THREADS) {
+          SLV[i] = MGV[i];
+          SLP[i] = MGP[i];
+        }
+      }
       Lcur += nsel;
       if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
       __syncthreads();

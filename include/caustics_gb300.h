@@ -234,13 +234,12 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
  *  chain (count + 1000 x iterations, first point included) and of the
  *  refinement (same encoding), theta of the limb points in limb order (room
  *  for the largest limb), clock cycles of the refinement's sub-phases:
- *  interval ranking and scan; new-point FP32 stages (FP64: whole solves); FP64
- *  polish and image filter; per-point labelling; faithful labelling; the new
- *  intervals' lengths and insertion; then of the initial sampling: limb
- *  solves; first-point labelling and step maps; chain repair and row
- *  permutation; then the ranking's key gathering alone (part of the
- *  refinement's first sub-phase); then FP32-stage iterations summed over the
- *  refinement points, and their number]. */
+ *  interval selection and scan; new-point FP32 stages (FP64: whole solves);
+ *  FP64 polish and image filter; per-point labelling; faithful labelling; the
+ *  new intervals' lengths, insertion and merge into the ranked intervals; then
+ *  of the initial sampling: limb solves; first-point labelling and step maps;
+ *  chain repair and row permutation; then FP32-stage iterations summed over
+ *  the refinement points, and their number]. */
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                               const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
 int64_t cgb_debug_record_len(int32_t npts_limb);
