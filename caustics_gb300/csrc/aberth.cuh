@@ -306,14 +306,15 @@ __device__ __forceinline__ bool roots_distinct(const cd (&z)[DEG]) {
 // degenerates and both can settle on one root.  warm (if given) is a start known
 // to separate the roots (e.g. the neighbouring limb point's roots plus jitter);
 // otherwise, or if that fails or merges roots, a cold start.  Returns the FP64
-// iteration count or -1.
+// iteration count or -1.  Not inlined: it runs rarely, and its body would
+// otherwise enter the register allocation of every kernel that can fall back.
 template <int DEG>
-__device__ int aberth64_fallback(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, const cd *warm) {
+__device__ __noinline__ int aberth64_fallback(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, const cd *warm) {
   int it = -1;
-  if (warm) {
+  if (warm) {  // a warm start converges in a few iterations or not at all
 #pragma unroll
     for (int i = 0; i < DEG; ++i) z[i] = warm[i];
-    it = aberth64<DEG>(p, z, itmax, true);
+    it = aberth64<DEG>(p, z, min(itmax, 64), true);
     if (it >= 0 && roots_distinct<DEG>(z)) return it;
   }
   it = aberth64<DEG>(p, z, itmax, false);
@@ -341,7 +342,13 @@ __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
 // Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
 // polynomial, FP64 Newton polish, FP64 fallback.  Returns the FP32 iteration
 // count, -1 on non-convergence; sets CGB_ST_FALLBACK in flags when used.
-template <int DEG>
+// WARM_FALLBACK: the FP64 fallback first starts from the roots found so far,
+// each moved by 1e-6 in its own direction (that separates a pair Newton merged;
+// a few FP64 steps then replace the tens of a cold start).  It suits the
+// one-polynomial-per-thread kernels, where a warp waits for its slowest lane;
+// in the contour kernel it measured slower (the chained matching that follows
+// ran 50 % longer with that code present), so that kernel starts cold.
+template <int DEG, bool WARM_FALLBACK = false>
 __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
   cf ph[DEG + 1], pl[DEG + 1];
   float alpha[DEG + 1];
@@ -451,7 +458,20 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   }
   if (!ok) {
     flags |= CGB_ST_FALLBACK;
-    if (aberth64_fallback<DEG>(p, z, itmax, nullptr) < 0) return -1;
+    if constexpr (WARM_FALLBACK) {
+      cd start[DEG];
+      bool finite = true;
+#pragma unroll
+      for (int i = 0; i < DEG; ++i) {
+        double sn, cs;
+        sincospi(2.0 * i / DEG, &sn, &cs);
+        start[i] = z[i] + mk(1e-6 * cs, 1e-6 * sn);
+        finite = finite && isfinite(start[i].x) && isfinite(start[i].y);
+      }
+      if (aberth64_fallback<DEG>(p, z, itmax, finite ? start : nullptr) < 0) return -1;
+    } else {
+      if (aberth64_fallback<DEG>(p, z, itmax, nullptr) < 0) return -1;
+    }
   }
   return it + 1;
 }

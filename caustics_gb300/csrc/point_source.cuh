@@ -23,7 +23,7 @@ constexpr int PS_THREADS = 128;
 
 template <int PREC, int DEG>
 __device__ __forceinline__ int solve(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
-  if constexpr (PREC == MIXED) return aberth_mixed<DEG>(p, z, itmax, warm, flags);
+  if constexpr (PREC == MIXED) return aberth_mixed<DEG, true>(p, z, itmax, warm, flags);
   else if constexpr (PREC == FP64_COMP) return aberth64_comp<DEG>(p, z, itmax, warm);
   else return aberth64<DEG>(p, z, itmax, warm);
 }
