@@ -6,16 +6,20 @@
 //  A  n0 = npts/2 limb points solved in parallel (cold start, one thread per
 //     point); rows put in the order of the reference's sequential warm-start
 //     chain: clear steps by nearest roots, ambiguous steps and the first point
-//     by the reference's own iteration (refea, bit-exact) on lane groups;
+//     by the reference's own iteration (refea, bit-exact) on lane groups (the
+//     first point's, in the batched path, by es_first_order_kernel ahead of
+//     this kernel);
 //  B  10 refinement rounds: gap per interval = max over images |dz| where either
 //     end is a real image, the n_add largest gaps (ties: larger index first, as
-//     argsort(...)[::-1]) get a midpoint point (extended_source.py:109-135),
-//     solved in parallel steps (coefficients per point; FP32 Aberth on a lane
-//     group per point; FP64 Newton and image filter per root; labelling per
-//     point against the left neighbour, the reference's warm start);
+//     argsort(...)[::-1]) get a midpoint point (extended_source.py:109-135);
+//     the intervals are ranked once and kept as a sorted list into which each
+//     round merges its new intervals; new points solved in parallel steps
+//     (coefficients per point; FP32 Aberth on a lane group per point; FP64
+//     Newton and image filter per root; labelling per point against the left
+//     neighbour, the reference's warm start);
 //  C  final chained matching over all limb points (extended_source.py:150-151):
-//     candidate rows sorted by distance in parallel, the greedy pass in integer
-//     arithmetic on one thread;
+//     candidate rows sorted by distance in parallel, the greedy pass on one
+//     warp (lane per track);
 //  D  tracks -> closed tracks / split open segments (extended_source.py:156-309),
 //     change points found in parallel;
 //  E  segment linking into <= 3 contours (extended_source.py:312-727);

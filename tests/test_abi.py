@@ -74,3 +74,34 @@ def test_no_cpu_fallback(lib):
         C.mag_point_source(np.array([0.1 + 0.1j]), s=0.9, q=0.1)
     with pytest.raises(L.CausticsError):
         C.mag_extended_source(0.1 + 0.1j, 1e-2, s=0.9, q=0.1)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The Python mirror's ctypes structures have the size and field offsets of
+    the C structs in include/caustics_gb300.h (a C program compiled against the
+    header reports them)."""
+    import shutil
+    import subprocess
+    from caustics_gb300 import _lib as L
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"cgb_lens_params": L.LensParams, "cgb_es_options": L.EsOptions, "cgb_curve_params": L.CurveParams}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "caustics_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(ROOT, "include")
+    cuda_inc = "/usr/local/cuda/include"
+    subprocess.run([cc, "-std=c11", "-I", inc, "-I", cuda_inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

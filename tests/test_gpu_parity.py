@@ -227,3 +227,16 @@ def test_mixed_fallback_near_double_root():
     ref = O.mag_extended_source(w[0], 0.028097114572181326, **kw)
     assert abs(m64[0] - ref) / ref < 1e-9
     assert abs(m32[0] - ref) / ref < 1e-6
+
+
+def test_mixed_fp32_stage_stall_point():
+    """A point of the bench light curve (s = 1.1, q = 5e-3, rho = 1e-2, LD,
+    npts_limb = 500) where one limb point's root sat just above the FP32
+    stopping rule's threshold and, before the FP32 stage was capped, ran the
+    FP32 loop toward itmax: the result must still match FP64 and converge."""
+    kw = dict(npts_limb=500, limb_darkening=True, u1=0.5, npts_ld=100, s=1.1, q=5e-3)
+    w = np.array([-0.11295772674510604 - 0.25366146120886357j])
+    m64 = C.mag_extended_source(w, 1e-2, precision="fp64", **kw)
+    m32, st = C.mag_extended_source(w, 1e-2, precision="mixed", return_status=True, **kw)
+    assert abs(m32[0] - m64[0]) / m64[0] < 1e-6
+    assert (int(st[0]) & 1) == 0  # CGB_ST_NOCONV
