@@ -170,6 +170,17 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q,
   uint32_t flags = 0;
   cd wi = w[i];
   wi.x += L.x_cm;
+  // Triple lenses always take the contour integral (lightcurve.py:226-227); for
+  // q < 0.01 the routing test is proximity & planetary (lightcurve.py:216-224),
+  // so where the planetary test fails the point takes the contour integral
+  // whatever its images give: neither the images nor the hexadecapole are
+  // needed (the contour kernel writes mag).
+  if (NL != 2 || (q < 0.01 && !planetary_test(L, wi, rho))) {
+    mag[i] = 0.0;
+    route[i] = 1;
+    if (status) status[i] = 0;
+    return;
+  }
   cd z[DEG];
   uint32_t m = images<PREC, NL>(L, wi, z, itmax, flags);
   double mu_multi = 0.0, dmu = 0.0;
@@ -187,7 +198,7 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q,
     }
     const cd(&z5)[5] = reinterpret_cast<const cd(&)[5]>(z);
     hex_ok = proximity_test_binary(L, wi, z5, m, rho, dmu);
-    if (q < 0.01) hex_ok = hex_ok && planetary_test(L, wi, rho);
+    // (q < 0.01: the planetary test passed above)
   }
   mag[i] = mu_multi;
   route[i] = hex_ok ? 0 : 1;
@@ -241,6 +252,16 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
   double sa, ca;
   sincos(cv.alpha, &sa, &ca);
   const cd wi = mk(cv.u0 * ca + tau * sa + L.x_cm, -cv.u0 * sa + tau * ca);
+  // for q < 0.01 the routing test is proximity & planetary (lightcurve.py:216-224):
+  // where the planetary test fails the point takes the contour integral whatever
+  // its images give, so it is queued without them (the contour kernel writes mag)
+  if (cv.q < 0.01 && !planetary_test(L, wi, cv.rho)) {
+    mag[i] = 0.0;
+    route[i] = 1;
+    if (status) status[i] = 0;
+    qlist[atomicAdd(qcount, 1ull)] = i;
+    return;
+  }
   uint32_t flags = 0;
   cd z[5];
   uint32_t m = images<PREC, 2>(L, wi, z, itmax, flags);
@@ -259,7 +280,7 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
     dmu += fabs(dq) + fabs(dh);
   }
   bool hex_ok = proximity_test_binary(L, wi, z, m, cv.rho, dmu);
-  if (cv.q < 0.01) hex_ok = hex_ok && planetary_test(L, wi, cv.rho);
+  // (q < 0.01: the planetary test passed above)
   mag[i] = mu_multi;
   route[i] = hex_ok ? 0 : 1;
   if (status) status[i] = flags;
