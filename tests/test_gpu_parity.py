@@ -240,3 +240,23 @@ def test_mixed_fp32_stage_stall_point():
     m32, st = C.mag_extended_source(w, 1e-2, precision="mixed", return_status=True, **kw)
     assert abs(m32[0] - m64[0]) / m64[0] < 1e-6
     assert (int(st[0]) & 1) == 0  # CGB_ST_NOCONV
+
+
+def test_routing_far_sources_small_q():
+    """q < 0.01: the point pass evaluates the planetary test first and sends a
+    point it rejects to the contour integral without solving its images; far
+    from the lenses the test passes and the images, hexadecapole and proximity
+    test decide as in the reference (lightcurve.py:216-224)."""
+    rng = np.random.default_rng(11)
+    s, q, rho = 1.1, 5e-3, 1e-2
+    w = 10 ** rng.uniform(0, 2.3, 64) * np.exp(1j * rng.uniform(0, 2 * np.pi, 64))
+    lens = O._lens_from_params(2, dict(s=s, q=q))
+    z, mask = O.images_point_source(w + lens.x_cm, lens)
+    mu, dmu = O.mag_hexadecapole(z, mask, rho, lens)
+    t1 = O.caustics_proximity_test(w + lens.x_cm, z, mask, rho, dmu, lens)
+    t2 = O.planetary_caustic_test(w + lens.x_cm, rho, lens)
+    test = t1 & t2
+    assert test.any() and (~test).any()
+    m, route = C.mag(w, rho, npts_limb=60, s=s, q=q, return_route=True)
+    assert np.array_equal(route, ~test)
+    assert np.max(np.abs(m[test] - mu[test]) / mu[test]) < 1e-10
