@@ -321,6 +321,24 @@ __device__ __noinline__ int aberth64_fallback(const cd (&p)[DEG + 1], cd (&z)[DE
   return (it >= 0 && roots_distinct<DEG>(z)) ? it : -1;
 }
 
+// The mixed solver's FP64 fallback from the roots it found: each moved by
+// 1e-6 in its own direction, which separates a pair Newton merged, so the FP64
+// iteration needs a few steps where a cold start needs tens; cold if that
+// fails.  Not inlined, like aberth64_fallback.
+template <int DEG>
+__device__ __noinline__ int aberth64_fallback_separated(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax) {
+  cd start[DEG];
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < DEG; ++i) {
+    double sn, cs;
+    sincospi(2.0 * i / DEG, &sn, &cs);
+    start[i] = z[i] + mk(1e-6 * cs, 1e-6 * sn);
+    finite = finite && isfinite(start[i].x) && isfinite(start[i].y);
+  }
+  return aberth64_fallback<DEG>(p, z, itmax, finite ? start : nullptr);
+}
+
 // FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
 // correction is at most 2^-40 |z|.
 template <int DEG, int SWEEPS = 3>
@@ -459,16 +477,7 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   if (!ok) {
     flags |= CGB_ST_FALLBACK;
     if constexpr (WARM_FALLBACK) {
-      cd start[DEG];
-      bool finite = true;
-#pragma unroll
-      for (int i = 0; i < DEG; ++i) {
-        double sn, cs;
-        sincospi(2.0 * i / DEG, &sn, &cs);
-        start[i] = z[i] + mk(1e-6 * cs, 1e-6 * sn);
-        finite = finite && isfinite(start[i].x) && isfinite(start[i].y);
-      }
-      if (aberth64_fallback<DEG>(p, z, itmax, finite ? start : nullptr) < 0) return -1;
+      if (aberth64_fallback_separated<DEG>(p, z, itmax) < 0) return -1;
     } else {
       if (aberth64_fallback<DEG>(p, z, itmax, nullptr) < 0) return -1;
     }

@@ -237,7 +237,7 @@ __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, 
 #pragma unroll
     for (int i = 0; i < DEG; ++i) z[i] = warm[i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
   }
-  int it = (PREC == MIXED) ? aberth_mixed<DEG>(p, z, P.itmax, warm != nullptr, flags)
+  int it = (PREC == MIXED) ? aberth_mixed<DEG, true>(p, z, P.itmax, warm != nullptr, flags)
                            : aberth64<DEG>(p, z, P.itmax, warm != nullptr);
   if (it < 0) flags |= CGB_ST_NOCONV;
   mkb = 0;
