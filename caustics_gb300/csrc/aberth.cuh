@@ -339,7 +339,53 @@ __device__ __noinline__ int aberth64_fallback_separated(const cd (&p)[DEG + 1], 
   return aberth64_fallback<DEG>(p, z, itmax, finite ? start : nullptr);
 }
 
-// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
+// FP64 Aberth iteration spread over a group of G lanes (G a power of two, DEG
+// <= G <= 32; every lane of the group calls it, gmask its lanes): lane r < DEG
+// owns root r (zr, from a start that separates the roots) and all roots update
+// together from the previous iterate; each root stops at the reference's FP64
+// rule.  Returns, uniformly over the group, whether every root stopped within
+// itmax iterations with finite values.
+template <int DEG, int G>
+__device__ bool aberth64_group(const cd (&p)[DEG + 1], cd &zr, int itmax, unsigned gmask) {
+  const int r = threadIdx.x & (G - 1);
+  double alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] = cabs(p[i]) * fma(3.8284271247461900976, (double)i, 1.0);
+  bool done = r >= DEG;
+  for (int it = 0; it < itmax; ++it) {
+    cd zall[DEG];
+#pragma unroll
+    for (int q = 0; q < DEG; ++q) zall[q] = mk(__shfl_sync(gmask, zr.x, q, G), __shfl_sync(gmask, zr.y, q, G));
+    if (!done) {
+      const double az = cabs(zr);
+      const bool rev = az > 1.0;
+      const cd x = rev ? crecip(zr) : zr;
+      cd h, hd;
+      double b;
+      horner_pair<DEG>(p, alpha, x, rev ? 1.0 / az : az, rev, h, hd, b);
+      if (cabs(h) > CGB_EPS64 * b) {
+        cd sum = mk(0.0, 0.0);
+#pragma unroll
+        for (int q = 0; q < DEG; ++q)
+          if (q != r) sum = sum + crecip(zr - zall[q]);
+        cd corr;
+        if (rev) {
+          const cd z2h = (zr * zr) * h, d = zr * h;
+          corr = cdiv(z2h, mk(d.x * DEG, d.y * DEG) - hd - z2h * sum);
+        } else {
+          corr = cdiv(h, hd - h * sum);
+        }
+        zr = zr - corr;
+      } else {
+        done = true;
+      }
+    }
+    if (__all_sync(gmask, done)) return __all_sync(gmask, isfinite(zr.x) && isfinite(zr.y));
+  }
+  return false;
+}
+
+// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
 // correction is at most 2^-40 |z|.
 template <int DEG, int SWEEPS = 3>
 __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {

@@ -1647,9 +1647,8 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           for (int j = tid / FG; j < nsel; j += ES_THREADS / FG) {
             const int slot = Lcur + j, sl = psl[j];
             cd *zrow = S.Z + (size_t)slot * DEG;
-            const uint32_t f = lg < DEG ? rflag[j * DEG + lg] : 1u;
-            bool ok = pok[j] != 0 && __all_sync(gmask, (f & 1u) != 0);
-            if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
+            uint32_t f = lg < DEG ? rflag[j * DEG + lg] : 1u;
+            auto distinct = [&]() {  // no two roots closer than 1e-7 of the largest modulus
               double scale = 0.0;
 #pragma unroll
               for (int q = 0; q < DEG; ++q) scale = fmax(scale, norm2(zrow[q]));
@@ -1657,9 +1656,40 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
               if (lg < DEG)
                 for (int q = lg + 1; q < DEG; ++q)
                   if (norm2(zrow[lg] - zrow[q]) < 1e-14 * scale) sep = false;
-              ok = __all_sync(gmask, sep);
+              return __all_sync(gmask, sep);
+            };
+            bool ok = pok[j] != 0 && __all_sync(gmask, (f & 1u) != 0);
+            if (ok) ok = distinct();  // (Newton alone may merge a near-double pair)
+            bool group_fb = false;
+            if (!ok) {
+              // FP64 fallback on the group first: simultaneous Aberth steps from
+              // the left neighbour's roots plus the jitter (the FP64 path's own
+              // start), one lane per root; then the filter per lane as above
+              cd p[DEG + 1];
+#pragma unroll
+              for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
+              cd zr = lg < DEG ? S.Z[(size_t)sl * DEG + lg] +
+                                     mk(1e-6 * ((lg & 1) ? 0.5 : -0.5), 1e-6 * ((lg & 2) ? 0.5 : -0.5))
+                               : mk(0.0, 0.0);
+              if (aberth64_group<DEG, FG>(p, zr, min(P.itmax, 64), gmask)) {
+                if (lg < DEG) zrow[lg] = zr;
+                __syncwarp(gmask);
+                if (distinct()) {
+                  f = 1u;
+                  if (lg < DEG) {
+                    double r, d;
+                    lens_filter<NL>(I.L, zr, pco[(size_t)j * (DEG + 2) + DEG + 1], r, d);
+                    if (r < 1e-6) f |= 2u;
+                    if (d > 0) f |= 4u;
+                    if (d == 0) f |= 8u;
+                    if (r > 1e-6 / 30 && r < 1e-6 * 30) f |= 16u;
+                  }
+                  ok = group_fb = true;
+                }
+              }
             }
             if (ok) {
+              if (group_fb && lg == 0) flags |= CGB_ST_FALLBACK;
               const uint32_t mkb = (__ballot_sync(gmask, lg < DEG && (f & 2u)) >> gbase) & all;
               const uint32_t pp = (__ballot_sync(gmask, lg < DEG && (f & 4u)) >> gbase) & all;
               const uint32_t zp = (__ballot_sync(gmask, lg < DEG && (f & 8u)) >> gbase) & all;
