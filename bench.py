@@ -40,10 +40,10 @@ UNIT = "evals/s"
 # npts_ld=G: L root solves (5.7e3 flop) + ~3.1 L contour points x 2G nodes x 60 flop
 FLOP_PER_EVAL = WL["npts_limb"] * 5.7e3 + 3.1 * WL["npts_limb"] * WL["npts_ld"] * 2 * 60
 # DRAM bytes (read + write) per evaluation of the contour kernel, from one ncu
-# capture of a 300-evaluation launch of this workload (1.57 MB per launch;
+# capture of a 300-evaluation launch of this workload (1.40 MB per launch;
 # instruction, constant and register-spill traffic: the inputs are 24 B per
 # evaluation), scaled by the evaluations of a launch
-DRAM_BYTES_PER_EVAL = 1.569e6 / 300
+DRAM_BYTES_PER_EVAL = 1.397e6 / 300
 
 
 def trajectory(n):
@@ -431,7 +431,7 @@ def main():
                      "peak_source": "measured live in bench.py (cgb_probe_fma, FP32 FMA burst); the path moves "
                                     "24 B per evaluation, so neither HBM nor tensor peaks bound it",
                      "flop_per_eval": FLOP_PER_EVAL,
-                     "pipes_ncu": {"fp64_pct_of_peak": 42.2, "fp32_fma_pct_of_peak": 8.7, "issue_active_pct": 17.4,
+                     "pipes_ncu": {"fp64_pct_of_peak": 42.5, "fp32_fma_pct_of_peak": 8.8, "issue_active_pct": 17.5,
                                    "source": "ncu --set full of a 300-evaluation launch of this workload "
                                              "(profiles/es_kernel_mixed_binary_ld_300pt.md): the FP64 pipe, not "
                                              "the FMA rate of the flop model, bounds the kernel"},
