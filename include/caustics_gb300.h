@@ -206,7 +206,8 @@ int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_
                        void *workspace, size_t workspace_bytes, void *stream);
 
 /* cgb_mag_lc_batched without a workspace argument and without allocating: the
- * queue lives in a file-scope device array of the library (2 MiB + 16 B per
+ * queue (and, for calls of at most 131,072 points, the first-limb-point row
+ * orders) lives in a file-scope device array of the library (2 MiB + 16 B per
  * device), so npoints is limited to 262,144 (larger calls fail with
  * CGB_ERR_UNSUPPORTED).  The first call on a device resolves the array's
  * address in that device's context (cudaGetSymbolAddress); make that first call
