@@ -64,6 +64,14 @@ def test_argument_checks_before_any_launch(lib):
     bad = L.LensParams(2, -1.0, 0.1, 0, 0, 0)
     assert lib.cgb_mag_point_source(None, None, None, None, 0, bad, 100, 0, None, None) == L.CGB_ERR_INVALID
     assert lib.cgb_ea_solve(None, None, None, 0, 5, 100, 0, None, None) == L.CGB_OK  # empty batch: no launch
+    # batched workspace: 16 + 16 n bytes asked for; below the queue alone (16 + 8 n) the call is refused
+    n = 100
+    assert lib.cgb_mag_lc_batched_workspace_bytes(n) == 16 + 16 * n
+    buf = np.zeros(64)
+    ptr = buf.ctypes.data_as(ctypes.c_void_p)
+    opts = L.EsOptions(200, 1, 0.5, 100, 2500, 1, 0, 1, 1, 0, 0.0)
+    rc = lib.cgb_mag_lc_batched(ptr, ptr, ptr, 1, n, ptr, ptr, None, ctypes.byref(opts), ptr, 16 + 8 * n - 1, None)
+    assert rc == L.CGB_ERR_INVALID and b"workspace" in lib.cgb_last_error()
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the behaviour without a CUDA device")
