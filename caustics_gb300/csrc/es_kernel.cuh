@@ -1188,6 +1188,9 @@ __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsPara
   __shared__ cd zs[NG][DEG];
   const int g = threadIdx.x / G, r = threadIdx.x & (G - 1);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) - r));
+  // the contour kernel may start its limb sampling now; it waits for this
+  // grid's completion (griddepcontrol.wait) before it reads perm0
+  asm volatile("griddepcontrol.launch_dependents;");
   const int64_t nitems = P.qhead ? *P.qcount : npoints;
   for (int64_t it = (int64_t)blockIdx.x * NG + g; it < nitems; it += (int64_t)gridDim.x * NG) {
     const int64_t pi = P.qhead ? P.qlist[it] : (index ? index[it] : it);
@@ -1361,7 +1364,10 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
         S.PERM[0] = ident;
       }
     } else if (P.perm0) {  // ordered ahead of this kernel (es_first_order_kernel)
-      if (tid == 0) S.PERM[0] = P.perm0[iord_sh];
+      if (tid == 0) {
+        asm volatile("griddepcontrol.wait;" ::: "memory");  // that grid complete (at once when launched after it)
+        S.PERM[0] = P.perm0[iord_sh];
+      }
     } else if (tid < RG) {
       int its;
       const uint64_t o = first_point_order_group<NL>(P, I, S.TH[0], S.Z, its);
@@ -2235,6 +2241,19 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
                                                                          const_cast<uint64_t *>(P.perm0));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    // programmatic dependent launch: the contour kernel starts while the
+    // ordering kernel runs and waits for it only where it reads perm0
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(ES_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, P, w0, index, route, n, mag, status);
   }
   k<<<grid, ES_THREADS, smem, stream>>>(P, w0, index, route, n, mag, status);
   return cudaGetLastError();
