@@ -67,16 +67,16 @@ def load_reference(ref_root):
     return lib, poly_roots
 
 
-def cfg1_points(n=10000):
-    # BASELINE workload "binary point source": x then y, each U[-1.5, 1.5], seed 0
+def binary_ps_points(n=10000):
+    # binary point-source workload (s = 0.9, q = 0.1): x then y, each U[-1.5, 1.5], seed 0
     rng = np.random.default_rng(0)
     x = rng.uniform(-1.5, 1.5, n)
     y = rng.uniform(-1.5, 1.5, n)
     return x + 1j * y
 
 
-def cfg3_systems(nsys, npts, seed=1):
-    # BASELINE workload "triple point source": per-system s1,s2~U[.5,2], q1~logU[1e-4,1],
+def triple_ps_systems(nsys, npts, seed=1):
+    # triple point-source workload: per-system s1,s2~U[.5,2], q1~logU[1e-4,1],
     # q2~logU[1e-4,1e-1], psi~U[0,2pi]; positions U[-1.5,1.5]^2 (x then y)
     rng = np.random.default_rng(seed)
     s1 = rng.uniform(0.5, 2.0, nsys)
@@ -198,7 +198,7 @@ def main():
     w = rng.uniform(-1.5, 1.5, 64) + 1j * rng.uniform(-1.5, 1.5, 64)
     cb = np.stack([np.asarray(ps._poly_coeffs_binary(w, a, e1)) for a, e1 in [(0.45, 1 / 1.1), (0.55, 0.9), (1.2, 0.5)]])
     out["coeffs_binary"] = dict(w=w, a=np.array([0.45, 0.55, 1.2]), e1=np.array([1 / 1.1, 0.9, 0.5]), coeffs=cb)
-    s1, s2, q1, q2, psi, wt = cfg3_systems(6, 16, seed=1)
+    s1, s2, q1, q2, psi, wt = triple_ps_systems(6, 16, seed=1)
     ct = []
     for k in range(6):
         a, e1 = 0.5 * s1[k], q1[k] / (1 + q1[k] + q2[k])
@@ -206,13 +206,13 @@ def main():
         ct.append(np.asarray(ps._poly_coeffs_triple(wt[k], a, r3, e1, e2)))
     out["coeffs_triple"] = dict(s1=s1, s2=s2, q1=q1, q2=q2, psi=psi, w=wt, coeffs=np.stack(ct))
 
-    # ---- roots: cfg1 polynomials through the reference solver (ehrlich_aberth.h) ----
-    wc = cfg1_points()[:2000]
+    # ---- roots: binary point-source polynomials through the reference solver (ehrlich_aberth.h) ----
+    wc = binary_ps_points()[:2000]
     a, q = 0.45, 0.1
     e1 = 1 / (1 + q)
     xcm = a * (1 - q) / (1 + q)
     coeffs = np.asarray(ps._poly_coeffs_binary(wc + xcm, a, e1))
-    out["roots_cfg1"] = dict(w=wc, coeffs=coeffs,
+    out["roots_binary_s0.9_q0.1"] = dict(w=wc, coeffs=coeffs,
                              roots_plain=np.asarray(poly_roots(coeffs, itmax=2500)),
                              roots_comp=np.asarray(poly_roots(coeffs, itmax=2500, compensated=True)))
     # the reference's own fixture (tests/test_ehrlich_aberth_primitive.py:19-27)
@@ -222,14 +222,14 @@ def main():
                                 roots_comp=np.asarray(poly_roots(cf, compensated=True)))
 
     # ---- point-source magnification (point_source.py:1762-1830) ----
-    wfull = cfg1_points()
-    out["mag_ps_cfg1"] = dict(w=wfull, s=np.float64(0.9), q=np.float64(0.1),
+    wfull = binary_ps_points()
+    out["mag_ps_binary_s0.9_q0.1"] = dict(w=wfull, s=np.float64(0.9), q=np.float64(0.1),
                               mag=np.asarray(ps.mag_point_source(wfull.copy(), nlenses=2, s=0.9, q=0.1)))
     xg = np.linspace(-0.5, 0.5, 50)
     wg = (xg[None, :] + 1j * xg[:, None]).reshape(-1)
     out["mag_ps_grid"] = dict(w=wg, s=np.float64(0.9), q=np.float64(0.2),
                               mag=np.asarray(ps.mag_point_source(wg.copy(), nlenses=2, s=0.9, q=0.2)))
-    s1, s2, q1, q2, psi, wt = cfg3_systems(8, 64, seed=1)
+    s1, s2, q1, q2, psi, wt = triple_ps_systems(8, 64, seed=1)
     mt, zt, mk = [], [], []
     for k in range(8):
         mt.append(np.asarray(ps.mag_point_source(wt[k].copy(), nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k], psi=psi[k])))
@@ -295,16 +295,16 @@ def main():
     for k, c in enumerate(cases):
         out[f"mag_es{k}"] = c
 
-    # ---- light curve (lightcurve.py:99-254): the cfg2 trajectory, every 100th point, and a q>0.01 curve ----
+    # ---- light curve (lightcurve.py:99-254): the 2000-point LD light curve (s 1.1, q 5e-3), every 100th point, and a q>0.01 curve ----
     t = np.linspace(-40.0, 40.0, 2000)
     tau = t / 20.0
     u0, alpha = 0.05, 0.6
     wtraj = (u0 * np.cos(alpha) + tau * np.sin(alpha)) + 1j * (-u0 * np.sin(alpha) + tau * np.cos(alpha))
     sub = wtraj[::100]
     mags = np.asarray(lc.mag(sub, 1e-2, nlenses=2, npts_limb=500, limb_darkening=True, u1=0.5, npts_ld=100, s=1.1, q=5e-3))
-    out["mag_lc_cfg2"] = dict(w=sub, rho=np.float64(1e-2), u1=np.float64(0.5), s=np.float64(1.1), q=np.float64(5e-3),
+    out["mag_lc_binary_ld_s1.1_q5e-3"] = dict(w=sub, rho=np.float64(1e-2), u1=np.float64(0.5), s=np.float64(1.1), q=np.float64(5e-3),
                               npts_limb=np.int64(500), npts_ld=np.int64(100), mag=mags)
-    print(f"[golden] mag cfg2 {time.time() - t0:.1f}s", flush=True)
+    print(f"[golden] mag LD light curve {time.time() - t0:.1f}s", flush=True)
     wq = np.linspace(-0.8, 0.8, 24) + 0.08j
     mags = np.asarray(lc.mag(wq, 2e-2, nlenses=2, npts_limb=200, limb_darkening=True, u1=0.4, npts_ld=60, s=0.95, q=0.3))
     out["mag_lc_q0.3"] = dict(w=wq, rho=np.float64(2e-2), u1=np.float64(0.4), s=np.float64(0.95), q=np.float64(0.3),

@@ -37,8 +37,8 @@ def ambiguous(z, w, lens):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_comp", "mixed"])
-def test_ea_solve_cfg1_roots(G, precision):
-    d = G("roots_cfg1")
+def test_ea_solve_binary_ps_roots(G, precision):
+    d = G("roots_binary_s0.9_q0.1")
     c = np.ascontiguousarray(d["coeffs"][:, ::-1])
     r = C.ehrlich_aberth(c, None, itmax=2500, precision=precision).reshape(c.shape[0], 5)
     assert setdist(r, d["roots_plain"]) < 1e-10
@@ -57,7 +57,7 @@ def test_poly_roots_reference_fixture(G, comp):
 
 
 def test_poly_roots_warm_start(G):
-    d = G("roots_cfg1")
+    d = G("roots_binary_s0.9_q0.1")
     c = d["coeffs"][:64]
     init = d["roots_plain"][:64] + 1e-3
     r = C.poly_roots(c, custom_init=True, roots_init=init)
@@ -78,7 +78,7 @@ def test_degree_4_6_10_random(precision):
 
 def test_legacy_xla_custom_call(G):
     """The reference's GPU custom-call ABI: buffers + packed descriptor."""
-    d = G("roots_cfg1")
+    d = G("roots_binary_s0.9_q0.1")
     c = torch.as_tensor(np.ascontiguousarray(d["coeffs"][:100, ::-1])).cuda()
     out = torch.empty((100 * 5,), dtype=torch.complex128, device="cuda")
     bufs = (ctypes.c_void_p * 2)(c.data_ptr(), out.data_ptr())
@@ -105,7 +105,7 @@ def test_invalid_arguments_rejected():
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_mag_point_source_binary(G, precision):
-    for name, s, q in (("mag_ps_cfg1", 0.9, 0.1), ("mag_ps_grid", 0.9, 0.2)):
+    for name, s, q in (("mag_ps_binary_s0.9_q0.1", 0.9, 0.1), ("mag_ps_grid", 0.9, 0.2)):
         d = G(name)
         m, z, mask, st = C.mag_point_source(d["w"], s=s, q=q, precision=precision, return_images=True,
                                             return_status=True)
@@ -162,7 +162,7 @@ def test_mag_extended_source_triple_golden(G, precision):
 
 @pytest.mark.parametrize("labelling", ["reference", "nearest"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", ["mag_lc_cfg2", "mag_lc_q0.3"])
+@pytest.mark.parametrize("name", ["mag_lc_binary_ld_s1.1_q5e-3", "mag_lc_q0.3"])
 def test_mag_light_curve_golden(G, name, precision, labelling):
     d = G(name)
     m, route = C.mag(d["w"], float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=True, u1=float(d["u1"]),

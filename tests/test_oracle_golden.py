@@ -32,7 +32,7 @@ def test_triple_coefficients(G):
 
 
 def test_roots_match_reference_solver(G):
-    d = G("roots_cfg1")
+    d = G("roots_binary_s0.9_q0.1")
     c = d["coeffs"][:, ::-1]
     r = O.ea_solve(c, itmax=2500, init_mode=1)
     assert np.max(np.abs(r - d["roots_plain"])) < 1e-12
@@ -62,7 +62,7 @@ def test_reference_fixture_residual(G):
 
 
 def test_mag_point_source_binary(G):
-    for name, s, q in (("mag_ps_cfg1", 0.9, 0.1), ("mag_ps_grid", 0.9, 0.2)):
+    for name, s, q in (("mag_ps_binary_s0.9_q0.1", 0.9, 0.1), ("mag_ps_grid", 0.9, 0.2)):
         d = G(name)
         m = O.mag_point_source(d["w"], s=s, q=q)
         assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
@@ -157,7 +157,7 @@ def test_mag_extended_source_triple(G):
     assert np.max(np.abs(m - d["mag"]) / d["mag"]) < 1e-9
 
 
-@pytest.mark.parametrize("name", ["mag_lc_cfg2", "mag_lc_q0.3"])
+@pytest.mark.parametrize("name", ["mag_lc_binary_ld_s1.1_q5e-3", "mag_lc_q0.3"])
 def test_mag_light_curve(G, name):
     d = G(name)
     m = O.mag(d["w"], float(d["rho"]), npts_limb=int(d["npts_limb"]), limb_darkening=True, u1=float(d["u1"]),
