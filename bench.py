@@ -408,11 +408,14 @@ def main():
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     buf = torch.empty(sms * 8, dtype=torch.float64, device=dev)
     import ctypes
+    from caustics_gb300 import build as B
+    probe = ctypes.CDLL(B.BENCH_LIB)  # benchmark-only FMA probe (csrc/bench/probe_fma.cu)
+    probe.cgb_probe_fma.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
 
     def fma_peak(fp64):
         iters, blocks = (4096, sms * 8) if not fp64 else (512, sms * 8)
-        launch = lambda: L.lib().cgb_probe_fma(fp64, iters, blocks, ctypes.c_void_p(buf.data_ptr()),
-                                               ctypes.c_void_p(stream.cuda_stream))
+        launch = lambda: probe.cgb_probe_fma(fp64, iters, blocks, ctypes.c_void_p(buf.data_ptr()),
+                                             ctypes.c_void_p(stream.cuda_stream))
         launch()
         return blocks * 256 * iters * 256 / (timed(stream, launch) * 1e-3) / 1e12
     fp32_peak = fma_peak(0)

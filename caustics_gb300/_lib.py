@@ -79,7 +79,6 @@ SIGNATURES = {
                                           ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
     "cgb_mag_lc_batched_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P,
                                               ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
-    "cgb_probe_fma": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -1,7 +1,10 @@
 """Build libcaustics_gb300.so in-tree with nvcc for sm_103a (GB300).
 
 Each translation unit in csrc/ is compiled in parallel, then linked into
-caustics_gb300/libcaustics_gb300.so.  Rebuilds only what changed.
+caustics_gb300/libcaustics_gb300.so (the C ABI of include/caustics_gb300.h).
+csrc/bench/ holds the benchmark's measurement probe, linked on its own into
+caustics_gb300/libcgb_bench.so so that the product library carries none of it.
+Rebuilds only what changed.
 
     python -m caustics_gb300.build [-v]
 """
@@ -16,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcaustics_gb300.so")
+BENCH_LIB = os.path.join(HERE, "libcgb_bench.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -45,15 +49,18 @@ def _deps_mtime():
 def build(verbose=False, jobs=None):
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_t = _deps_mtime()
     todo = []
-    objs = []
-    for src in sources:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        objs.append(obj)
-        if not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_t):
-            todo.append((src, obj))
+    libs = []
+    for lib, sources in ((LIB, sorted(glob.glob(os.path.join(CSRC, "*.cu")))),
+                         (BENCH_LIB, sorted(glob.glob(os.path.join(CSRC, "bench", "*.cu"))))):
+        objs = []
+        for src in sources:
+            obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+            objs.append(obj)
+            if not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_t):
+                todo.append((src, obj))
+        libs.append((lib, objs))
 
     def compile_one(job):
         src, obj = job
@@ -71,16 +78,17 @@ def build(verbose=False, jobs=None):
             for done in ex.map(compile_one, todo):
                 if verbose:
                     print("compiled", os.path.basename(done), flush=True)
-    if todo or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        libdir = _cuda_lib_dir(nvcc)
-        cmd = [nvcc] + ARCH + ["-shared", "--cudart", "shared", "-o", LIB + ".tmp"] + objs + [
-            "-Xlinker", f"-rpath,{libdir}"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(LIB + ".tmp", LIB)
+    libdir = _cuda_lib_dir(nvcc)
+    for lib, objs in libs:
+        if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+            cmd = [nvcc] + ARCH + ["-shared", "--cudart", "shared", "-o", lib + ".tmp"] + objs + [
+                "-Xlinker", f"-rpath,{libdir}"]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link of {os.path.basename(lib)} failed:\n{r.stdout}\n{r.stderr}")
+            os.replace(lib + ".tmp", lib)
     return LIB
 
 

@@ -1,12 +1,17 @@
-// Throughput probe for the roofline denominators of the magnification kernels:
-// FP32 / FP64 fused multiply-add issue rate of the whole GPU.  The kernels of
-// this library are SIMT arithmetic (no dense contraction, negligible HBM
-// traffic), so their roofline is the FMA pipe, measured here on the same
-// device and clocks as the timed kernels.
+// Throughput probe for the roofline denominators of the magnification kernels
+// (benchmark-only library libcgb_bench.so, not part of the C ABI): FP32 / FP64
+// fused multiply-add issue rate of the whole GPU.  The magnification kernels
+// are SIMT arithmetic (no dense contraction, negligible HBM traffic), so their
+// roofline is the FMA pipe, measured here on the same device and clocks as the
+// timed kernels.
+//
+//   int cgb_probe_fma(int fp64, int iters, int blocks, void *out, void *stream)
+// launches `blocks` CTAs of 256 threads, each thread running iters*16*8
+// independent fused multiply-adds in FP32 (fp64 = 0) or FP64; flops =
+// blocks*256*iters*256.  `out` needs one element per block (never written in
+// practice).  Returns 0, or 1 (bad arguments) / 2 (launch error).
 #include <cuda_runtime.h>
 #include <stdint.h>
-
-#include "../../include/caustics_gb300.h"
 
 namespace {
 
@@ -36,11 +41,11 @@ __global__ void fma_probe(int iters, T seed, T *out) {
 }  // namespace
 
 extern "C" int cgb_probe_fma(int32_t fp64, int32_t iters, int32_t blocks, void *out, void *stream) {
-  if (iters < 1 || blocks < 1 || !out) return CGB_ERR_INVALID;
+  if (iters < 1 || blocks < 1 || !out) return 1;
   cudaStream_t s = (cudaStream_t)stream;
   if (fp64)
     fma_probe<double><<<blocks, 256, 0, s>>>(iters, 1.0, (double *)out);
   else
     fma_probe<float><<<blocks, 256, 0, s>>>(iters, 1.0f, (float *)out);
-  return cudaGetLastError() == cudaSuccess ? CGB_OK : CGB_ERR_CUDA;
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

@@ -245,13 +245,6 @@ int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double r
                               const cgb_es_options *opts, uint32_t *status, double *dbg, void *stream);
 int64_t cgb_debug_record_len(int32_t npts_limb);
 
-/* Measurement utility (no counterpart in the reference): launches `blocks`
- * CTAs of 256 threads, each thread running iters*16*8 dependent-free fused
- * multiply-adds in FP32 (fp64 = 0) or FP64; flops = blocks*256*iters*256.
- * `out` needs one element per block (never written in practice).  Used as the
- * live FMA-pipe roofline denominator of the SIMT kernels. */
-int cgb_probe_fma(int32_t fp64, int32_t iters, int32_t blocks, void *out, void *stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,12 @@ Known deviations of this harness from the reference under real JAX:
 * roots come from the reference's C++ solver through ctypes instead of an XLA
   custom call (identical code, compiled with g++ -O2 -DNDEBUG).
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference] [--only roots_jvp|likelihood|parallax]
+The reference checkout is --ref, else $CAUSTICS_REF, else a directory named
+`reference` beside this repository.
+
+Usage:  python tests/golden/make_golden.py [--ref CHECKOUT] [--only NAME] [--procs N]
+        (NAME: one fixture group, e.g. roots_jvp, likelihood, parallax, lc_2000pt,
+        batched_seed2, batched_seed2_flagged, vjp_seed3, triple_ps_1000sys, hex_triple)
 """
 import argparse
 import ctypes
@@ -31,6 +36,13 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def default_reference():
+    for cand in (os.environ.get("CAUSTICS_REF"), os.path.join(os.path.dirname(REPO), "reference")):
+        if cand and os.path.isdir(os.path.join(cand, "src", "caustics")):
+            return cand
+    return None
 
 
 def load_reference(ref_root):
@@ -170,12 +182,294 @@ def parallax_fixture():
     return out
 
 
+# ---------------------------------------------------------------------------
+# Fixtures at the configured workload sizes.  The reference evaluates one
+# extended-source point in ~0.2-0.35 s on the stand-in, so these spread the
+# points over a spawn pool whose workers each load the reference.
+# ---------------------------------------------------------------------------
+
+def _worker_init(ref_root):
+    load_reference(ref_root)
+
+
+def pool_map(fn, jobs, ref_root, procs):
+    import multiprocessing as mp
+    if procs <= 1:
+        _worker_init(ref_root)
+        return [fn(j) for j in jobs]
+    with mp.get_context("spawn").Pool(procs, initializer=_worker_init, initargs=(ref_root,)) as pool:
+        return pool.map(fn, jobs, chunksize=1)
+
+
+def _job_lc_mag(job):
+    """The reference's mag() (lightcurve.py:99-254) on a chunk of source positions."""
+    w, rho, kw = job
+    from caustics import lightcurve as lc
+    return np.asarray(lc.mag(np.asarray(w), rho, nlenses=2, **kw), dtype=np.float64)
+
+
+def _job_triple_ps(job):
+    """mag_point_source and the image solve of one triple system (point_source.py:1652-1830)."""
+    w, s, q, q3, r3, psi = job
+    from caustics import point_source as ps
+    a, e1 = 0.5 * s, q / (1 + q + q3)
+    e2, r3c, xcm = q * e1, r3 * np.exp(1j * psi), 0.5 * s * (1 - q) / (1 + q)
+    mag = np.asarray(ps.mag_point_source(w.copy(), nlenses=3, s=s, q=q, q3=q3, r3=r3, psi=psi))
+    z, m = ps._images_point_source(w + xcm, nlenses=3, a=a, r3=r3c, e1=e1, e2=e2)
+    return mag, np.asarray(z), np.asarray(m)
+
+
+def _job_es_triple(job):
+    w0, rho, kw = job
+    from caustics import extended_source as es
+    return float(es.mag_extended_source(w0, rho, nlenses=3, **kw))
+
+
+def lc_mag_pooled(w, rho, kw, ref_root, procs, chunk=25):
+    w = np.asarray(w)
+    jobs = [(w[i:i + chunk], rho, kw) for i in range(0, len(w), chunk)]
+    return np.concatenate(pool_map(_job_lc_mag, jobs, ref_root, procs)) if len(w) else np.zeros(0)
+
+
+def reference_route(w, rho, s, q):
+    """The reference's routing in mag() (lightcurve.py:200-224), from its own
+    pieces: True where the point takes the contour integral."""
+    from caustics import lightcurve as lc
+    from caustics import multipole as mp
+    from caustics import point_source as ps
+    a, e1 = 0.5 * s, 1 / (1 + q)
+    xcm = a * (1 - q) / (1 + q)
+    wc = np.asarray(w) + xcm
+    z, m = ps._images_point_source(wc, nlenses=2, roots_itmax=2500, a=a, e1=e1)
+    _, dmu = mp._mag_hexadecapole(z, m, rho, nlenses=2, a=a, e1=e1)
+    t1 = np.asarray(lc._caustics_proximity_test(wc, z, m, rho, dmu, nlenses=2, a=a, e1=e1))
+    t2 = np.asarray(lc._planetary_caustic_test(wc, rho, a=a, e1=e1))
+    return ~((t1 & t2) if q < 0.01 else t1)
+
+
+def trajectory_points(t, cv):
+    """w(t) of one curve (s, q, rho, u1, u0, alpha, t0, tE): the rectilinear
+    part of trajectory.py:152-155 (pi_E = 0)."""
+    u0, al, t0, te = cv[4], cv[5], cv[6], cv[7]
+    tau = (np.asarray(t) - t0) / te
+    return (u0 * np.cos(al) + tau * np.sin(al)) + 1j * (-u0 * np.sin(al) + tau * np.cos(al))
+
+
+def batched_workload(seed, ncurves, nmin, nmax):
+    sys.path.insert(0, REPO)
+    from bench import draw_batched
+    return draw_batched(ncurves, seed, nmin, nmax, ncurves)
+
+
+def lc_2000pt_fixture(ref, procs):
+    """Every point of the 2000-point limb-darkened light curve (s 1.1, q 5e-3,
+    rho 1e-2, u1 0.5, npts_limb 500, npts_ld 100, u0 0.05, alpha 0.6, t0 0,
+    tE 20, t uniform on [-40, 40])."""
+    t = np.linspace(-40.0, 40.0, 2000)
+    cv = np.array([1.1, 5e-3, 1e-2, 0.5, 0.05, 0.6, 0.0, 20.0])
+    w = trajectory_points(t, cv)
+    kw = dict(npts_limb=500, limb_darkening=True, u1=0.5, npts_ld=100, s=1.1, q=5e-3)
+    mag = lc_mag_pooled(w, 1e-2, kw, ref, procs)
+    return {"mag_lc_binary_ld_s1.1_q5e-3_2000pt": dict(t=t, w=w, curve=cv, npts_limb=np.int64(500),
+                                                       npts_ld=np.int64(100), mag=mag,
+                                                       route=reference_route(w, 1e-2, 1.1, 5e-3))}
+
+
+def _batched_points_fixture(off, t, cv, curve_ids, ref, procs):
+    """mag() of the given curves of a batched workload, npts_limb 200, npts_ld
+    100, limb darkened with each curve's u1."""
+    ts, mags, routes, lens = [], [], [], []
+    for c in curve_ids:
+        tc = t[off[c]:off[c + 1]]
+        w = trajectory_points(tc, cv[c])
+        kw = dict(npts_limb=200, limb_darkening=True, u1=float(cv[c, 3]), npts_ld=100, s=float(cv[c, 0]),
+                  q=float(cv[c, 1]))
+        mags.append(lc_mag_pooled(w, float(cv[c, 2]), kw, ref, procs))
+        routes.append(reference_route(w, float(cv[c, 2]), float(cv[c, 0]), float(cv[c, 1])))
+        ts.append(tc)
+        lens.append(len(tc))
+        print(f"[golden] curve {c}: {len(tc)} points, {int(routes[-1].sum())} contour", flush=True)
+    return dict(curve_ids=np.asarray(curve_ids, dtype=np.int64), offsets=np.concatenate([[0], np.cumsum(lens)]).astype(
+        np.int64), t=np.concatenate(ts), curves=cv[np.asarray(curve_ids)], mag=np.concatenate(mags),
+        route=np.concatenate(routes), npts_limb=np.int64(200), npts_ld=np.int64(100))
+
+
+def batched_seed2_fixture(ref, procs):
+    """Whole curves of the 4096-curve workload (seed 2, lengths U{200..5000}):
+    the two shortest with q < 1e-3, with 1e-3 <= q < 1e-2 and with q >= 1e-2,
+    and the shortest curve of at least 2000 points with q >= 1e-2."""
+    off, t, cv = batched_workload(2, 4096, 200, 5000)
+    lens, q = np.diff(off), cv[:, 1]
+    pick = []
+    for lo, hi in [(0.0, 1e-3), (1e-3, 1e-2), (1e-2, 2.0)]:
+        idx = np.flatnonzero((q >= lo) & (q < hi))
+        pick += [int(c) for c in idx[np.argsort(lens[idx], kind="stable")][:2]]
+    idx = np.flatnonzero((q >= 1e-2) & (lens >= 2000))
+    pick.append(int(idx[np.argmin(lens[idx])]))
+    return {"mag_lc_batched_seed2_sample": _batched_points_fixture(off, t, cv, pick, ref, procs)}
+
+
+def batched_seed2_flagged_fixture(ref, procs, flagged):
+    """Single points of the 4096-curve workload (seed 2) given by their point
+    index: the points whose evaluation set a non-convergence or contour-linking
+    status bit in a full run of the GPU path."""
+    off, t, cv = batched_workload(2, 4096, 200, 5000)
+    pts = np.unique(np.asarray(flagged, dtype=np.int64))
+    cid = np.searchsorted(off, pts, side="right") - 1
+    ws = np.array([trajectory_points(t[i:i + 1], cv[c])[0] for i, c in zip(pts, cid)])
+    jobs = [(ws[k:k + 1], float(cv[c, 2]), dict(npts_limb=200, limb_darkening=True, u1=float(cv[c, 3]), npts_ld=100,
+                                                s=float(cv[c, 0]), q=float(cv[c, 1])))
+            for k, c in enumerate(cid)]
+    mags = np.concatenate(pool_map(_job_lc_mag, jobs, ref, procs))
+    route = np.array([reference_route(ws[k:k + 1], float(cv[c, 2]), float(cv[c, 0]), float(cv[c, 1]))[0]
+                      for k, c in enumerate(cid)])
+    return {"mag_lc_batched_seed2_flagged": dict(point_ids=pts, curve_ids=cid, t=t[pts], curves=cv[cid], mag=mags,
+                                                 route=route, npts_limb=np.int64(200), npts_ld=np.int64(100))}
+
+
+def vjp_seed3_fixture(ref, procs, curve_ids=(3, 8, 5, 9)):
+    """Per-point derivatives of the reference's mag() with respect to
+    (s, q, rho, u1, Re w, Im w) by central differences at two steps, on four
+    whole curves (1000 points each) of the 256-curve gradient workload (seed 3):
+    curves 3 and 8 (q >= 0.01) and 5 and 9 (q < 0.01, every point through the
+    contour integral).  Steps: h * |parameter| for s, q, rho, u1 and h * rho for
+    the source position, h = 1e-7 and 1e-8; a derivative is trusted where the
+    two steps agree (the discrete limb refinement can change between +-h)."""
+    off, t, cv = batched_workload(3, 256, 1000, 1000)
+    steps = (1e-7, 1e-8)
+    out = {"curve_ids": np.asarray(curve_ids, dtype=np.int64), "steps": np.asarray(steps)}
+    jobs, keys = [], []
+    chunk = 50
+    for c in curve_ids:
+        w = trajectory_points(t[off[c]:off[c + 1]], cv[c])
+        base = dict(npts_limb=200, limb_darkening=True, u1=float(cv[c, 3]), npts_ld=100, s=float(cv[c, 0]),
+                    q=float(cv[c, 1]))
+        rho = float(cv[c, 2])
+        variants = [("base", 0, 0.0, 0)]
+        for x in range(6):
+            for h in steps:
+                for sg in (1, -1):
+                    variants.append(("d", x, h, sg))
+        for v in variants:
+            _, x, h, sg = v
+            kw, r, ww = dict(base), rho, w
+            if v[0] == "d":
+                if x == 0:
+                    kw["s"] = base["s"] * (1 + sg * h)
+                elif x == 1:
+                    kw["q"] = base["q"] * (1 + sg * h)
+                elif x == 2:
+                    r = rho * (1 + sg * h)
+                elif x == 3:
+                    kw["u1"] = base["u1"] * (1 + sg * h)
+                else:
+                    ww = w + sg * h * rho * (1.0 if x == 4 else 1j)
+            for i in range(0, len(w), chunk):
+                jobs.append((ww[i:i + chunk], r, kw))
+                keys.append((c, v, i))
+    res = pool_map(_job_lc_mag, jobs, ref, procs)
+    got = {}
+    for k, m in zip(keys, res):
+        got.setdefault((k[0], k[1]), []).append((k[2], m))
+    for c in curve_ids:
+        cat = lambda v: np.concatenate([m for _, m in sorted(got[(c, v)], key=lambda e: e[0])])
+        mag = cat(("base", 0, 0.0, 0))
+        J = np.zeros((2, len(mag), 6))
+        scale = [cv[c, 0], cv[c, 1], cv[c, 2], cv[c, 3], cv[c, 2], cv[c, 2]]
+        for x in range(6):
+            for hi, h in enumerate(steps):
+                J[hi, :, x] = (cat(("d", x, h, 1)) - cat(("d", x, h, -1))) / (2 * h * scale[x])
+        w = trajectory_points(t[off[c]:off[c + 1]], cv[c])
+        out[f"t{c}"] = t[off[c]:off[c + 1]]
+        out[f"curve{c}"] = cv[c]
+        out[f"mag{c}"] = mag
+        out[f"jac{c}"] = J
+        out[f"route{c}"] = reference_route(w, float(cv[c, 2]), float(cv[c, 0]), float(cv[c, 1]))
+    return {"vjp_seed3_fd": out}
+
+
+def triple_ps_1000sys_fixture(ref, procs, npos=32, nroots=2):
+    """Triple-lens point source over all 1000 systems of the triple workload
+    (seed 1: s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4, 1e-1],
+    psi ~ U[0, 2 pi]; 1000 positions per system, x then y ~ U[-1.5, 1.5]; the
+    reference keywords s = s1, q = q1, q3 = q2, r3 = s2): magnifications and
+    image counts of the first `npos` positions of every system, and roots with
+    their image mask for the first `nroots`."""
+    s1, s2, q1, q2, psi, w = triple_ps_systems(1000, 1000, seed=1)
+    jobs = [(w[k, :npos].copy(), s1[k], q1[k], q2[k], s2[k], psi[k]) for k in range(1000)]
+    res = pool_map(_job_triple_ps, jobs, ref, procs)
+    mag = np.stack([r[0] for r in res])
+    nimg = np.stack([r[2].sum(axis=0) for r in res]).astype(np.uint8)
+    roots = np.stack([r[1][:, :nroots].T for r in res])  # [sys, pos, 10]
+    mask = np.stack([r[2][:, :nroots].T for r in res])
+    return {"mag_ps_triple_1000sys": dict(npos=np.int64(npos), mag=mag, nimg=nimg, roots=roots, mask=mask)}
+
+
+def hex_triple_fixture(ref, procs):
+    """The reference's triple-lens hexadecapole (multipole.py:208-244) and the
+    triple branch of its proximity test (lightcurve.py:23-75, third lens term
+    (z + r3) as written there) on points near the caustics and elsewhere.  The
+    reference's mag() never calls them for triple lenses (lightcurve.py:226-227)
+    and fails on an undefined name after them (:252), so they are run directly,
+    on the same inputs mag() would give them.  mag_full: the reference's
+    uniform-source mag_extended_source (npts_limb 200) at up to 12 points per
+    system that the test accepts, to show the hexadecapole's accuracy there."""
+    from caustics import lightcurve as lc
+    from caustics import multipole as mp
+    from caustics import point_source as ps
+    s1, s2, q1, q2, psi, _ = triple_ps_systems(1000, 1, seed=1)
+    e1 = q1 / (1 + q1 + q2)
+    e3 = 1 - e1 - q1 * e1
+    systems = [(1.0, 0.5, 0.05, 0.9, 1.1, 1e-2)]
+    good = np.flatnonzero((np.minimum(np.minimum(e1, q1 * e1), e3) >= 1e-2))[:2]
+    small = np.flatnonzero(np.minimum(np.minimum(e1, q1 * e1), e3) < 1e-2)[:1]
+    for k, rho in zip(list(good) + list(small), (1e-2, 3e-3, 3e-3)):
+        systems.append((s1[k], q1[k], q2[k], s2[k], psi[k], rho))
+    out = {}
+    for n, (s, q, q3, r3, ps_, rho) in enumerate(systems):
+        a, ee1 = 0.5 * s, q / (1 + q + q3)
+        ee2, r3c, xcm = q * ee1, r3 * np.exp(1j * ps_), 0.5 * s * (1 - q) / (1 + q)
+        _, cau = ps.critical_and_caustic_curves(npts=100, nlenses=3, s=s, q=q, q3=q3, r3=r3, psi=ps_)
+        rng = np.random.default_rng(50 + n)
+        wpts = np.concatenate([near_caustic_points(cau, 10 * rho, 60, seed=60 + n),
+                               rng.uniform(-1, 1, 20) + 1j * rng.uniform(-1, 1, 20)])
+        prm = dict(a=a, r3=r3c, e1=ee1, e2=ee2)
+        z, m = ps._images_point_source(wpts + xcm, nlenses=3, **prm)
+        mu, dmu = mp._mag_hexadecapole(z, m, rho, nlenses=3, **prm)
+        t1 = np.asarray(lc._caustics_proximity_test(wpts + xcm, z, m, rho, dmu, nlenses=3, **prm))
+        acc = np.flatnonzero(t1)[:12]
+        mfull = pool_map(_job_es_triple, [(wpts[i], rho, dict(npts_limb=200, s=s, q=q, q3=q3, r3=r3, psi=ps_))
+                                          for i in acc], ref, procs)
+        out[f"hex_triple{n}"] = dict(s=np.float64(s), q=np.float64(q), q3=np.float64(q3), r3=np.float64(r3),
+                                     psi=np.float64(ps_), rho=np.float64(rho), w=wpts, z=np.asarray(z),
+                                     mask=np.asarray(m), mu_multi=np.asarray(mu), delta_mu=np.asarray(dmu),
+                                     test_prox=t1, full_idx=acc, mag_full=np.asarray(mfull))
+        print(f"[golden] triple hexadecapole system {n}: {int(t1.sum())} of {len(t1)} accepted", flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="write only this fixture (roots_jvp, likelihood, parallax)")
+    ap.add_argument("--ref", default=default_reference())
+    ap.add_argument("--only", default=None, help="write only this fixture group (see the module docstring)")
+    ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--flagged", default=None, help="batched_seed2_flagged: .npy of point indices")
     args = ap.parse_args()
+    if args.ref is None:
+        raise SystemExit("no reference checkout: pass --ref or set CAUSTICS_REF")
+    big = {"lc_2000pt": lambda: lc_2000pt_fixture(args.ref, args.procs),
+           "batched_seed2": lambda: batched_seed2_fixture(args.ref, args.procs),
+           "batched_seed2_flagged": lambda: batched_seed2_flagged_fixture(args.ref, args.procs, np.load(args.flagged)),
+           "vjp_seed3": lambda: vjp_seed3_fixture(args.ref, args.procs),
+           "triple_ps_1000sys": lambda: triple_ps_1000sys_fixture(args.ref, args.procs),
+           "hex_triple": lambda: hex_triple_fixture(args.ref, args.procs)}
     lib, poly_roots = load_reference(args.ref)
+    if args.only in big:
+        t0 = time.time()
+        for name, d in big[args.only]().items():
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+            print(f"[golden] wrote {name} in {time.time() - t0:.1f}s", flush=True)
+        return
     from caustics import point_source as ps
     if args.only == "roots_jvp":
         np.savez_compressed(os.path.join(HERE, "roots_jvp.npz"), **roots_jvp_fixture(poly_roots, ps))
