@@ -2,7 +2,8 @@
 fbartolic/caustics — Ehrlich-Aberth root solver, point-source and
 extended-source (contour-integration) magnification, hexadecapole routing —
 behind a C ABI (include/caustics_gb300.h) with the reference's Python
-signatures."""
+signatures, and as torch operators (torch.ops.caustics.*, caustics_gb300.ops)."""
+from . import ops  # noqa: F401  (registers the torch operators)
 from .api import (  # noqa: F401
     AnnualParallaxTrajectory,
     BatchedLightCurves,
