@@ -17,6 +17,7 @@ from .api import (  # noqa: F401
     mag_lc_batched_vjp,
     lens_eq,
     lens_eq_det_jac,
+    lens_polynomial,
     mag,
     mag_extended_source,
     mag_point_source,
@@ -28,7 +29,7 @@ from .api import (  # noqa: F401
     roots_vjp,
 )
 
-__all__ = ["ehrlich_aberth", "poly_roots", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
+__all__ = ["ehrlich_aberth", "poly_roots", "lens_polynomial", "lens_eq", "lens_eq_det_jac", "mag_point_source", "mag_extended_source",
            "mag", "mag_extended_source_grad", "mag_lc_batched", "mag_lc_batched_vjp", "LightCurveMagnification", "BatchedLightCurves",
            "roots_jvp", "roots_vjp", "critical_and_caustic_curves",
            "marginalized_log_likelihood", "marginalized_log_likelihood_batched", "LightCurveLogLikelihood",

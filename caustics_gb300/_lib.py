@@ -25,6 +25,7 @@ ST_AMBIGUOUS = 2
 ST_FALLBACK = 4
 ST_MERGE = 8
 ST_CAPACITY = 16
+ST_INVALID = 32
 
 
 class LensParams(ctypes.Structure):
@@ -36,7 +37,8 @@ class EsOptions(ctypes.Structure):
     _fields_ = [("npts_limb", ctypes.c_int32), ("limb_darkening", ctypes.c_int32), ("u1", ctypes.c_double),
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32),
-                ("labelling", ctypes.c_int32), ("grad_fp64_above", ctypes.c_double)]
+                ("labelling", ctypes.c_int32), ("grad_fp64_above", ctypes.c_double),
+                ("triple_routing", ctypes.c_int32)]
 
 
 class CurveParams(ctypes.Structure):
@@ -51,6 +53,7 @@ SIGNATURES = {
     "cgb_gauss_legendre": (ctypes.c_int, [ctypes.c_int32, _P, _P]),
     "cgb_ea_solve": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "gpu_ehrlich_aberth": (None, [_P, _P, ctypes.c_char_p, ctypes.c_size_t]),
+    "cgb_lens_polynomial": (ctypes.c_int, [_P, _P, ctypes.c_int64, LensParams, _P]),
     "cgb_parallax_trajectory": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
                                                _P, _P]),
@@ -73,6 +76,7 @@ SIGNATURES = {
                                                  ctypes.POINTER(EsOptions), _P, _P, _P]),
     "cgb_debug_record_len": (ctypes.c_int64, [ctypes.c_int32]),
     "cgb_mag_lc_batched_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+    "cgb_mag_lc_batched_vjp_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
     "cgb_mag_lc_batched_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
                                                   ctypes.POINTER(EsOptions), _P]),
     "cgb_mag_lc_batched": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,

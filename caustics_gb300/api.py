@@ -221,6 +221,22 @@ def _lens_geometry(nlenses, params):
     raise ValueError("`nlenses` has to be set to be <= 3.")
 
 
+def lens_polynomial(w, nlenses=2, **params):
+    """Coefficients complex128 [..., nlenses^2 + 2], low -> high, of the
+    lens-equation polynomial of each source position w (the frame of
+    mag_point_source, shifted by x_cm): the reference's _poly_coeffs_binary /
+    _poly_coeffs_triple (point_source.py:17-86, 89-1479; highest order first
+    there) in product form, on the GPU (cgb_lens_polynomial)."""
+    wt, was_np = _to_device(w, torch.complex128)
+    wf = wt.reshape(-1).contiguous()
+    deg = nlenses * nlenses + 1
+    c = torch.empty((wf.numel(), deg + 1), dtype=torch.complex128, device=wf.device)
+    with torch.cuda.device(wf.device):
+        L.check(L.lib().cgb_lens_polynomial(_ptr(wf), _ptr(c), wf.numel(), L.lens_params(nlenses, params), _stream()),
+                "cgb_lens_polynomial")
+    return _out(c.reshape(tuple(wt.shape) + (deg + 1,)), was_np)
+
+
 def lens_eq(z, nlenses=2, **params):
     """w = z - sum_j eps_j / (conj(z) - conj(r_j)) with the reference's
     (a, e1[, e2, r3]) parameters (point_source.py:1536-1556)."""
@@ -276,13 +292,18 @@ def mag_point_source(w, nlenses=2, roots_itmax=2500, roots_compensated=False, pr
 _LABELLING = {"reference": 0, "nearest": 1}
 
 
+_TRIPLE_ROUTING = {"contour": 0, "reference": 1, "corrected": 2}
+
+
 def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1,
-                grad_fp64_above=0.0, labelling="reference"):
+                grad_fp64_above=0.0, labelling="reference", triple_routing="contour"):
     if labelling not in _LABELLING:
         raise ValueError(f"labelling must be one of {sorted(_LABELLING)}")
+    if triple_routing not in _TRIPLE_ROUTING:
+        raise ValueError(f"triple_routing must be one of {sorted(_TRIPLE_ROUTING)}")
     return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
                        _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group),
-                       _LABELLING[labelling], float(grad_fp64_above))
+                       _LABELLING[labelling], float(grad_fp64_above), _TRIPLE_ROUTING[triple_routing])
 
 
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
@@ -312,9 +333,15 @@ def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False,
 
 def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, npts_ld=100, roots_itmax=2500,
         roots_compensated=False, precision=None, return_route=False, return_status=False, grid=0,
-        labelling="reference", **params):
+        labelling="reference", triple_routing="contour", **params):
     """Light curve: hexadecapole where the reference's tests accept it, contour
-    integration elsewhere (lightcurve.py:99-254)."""
+    integration elsewhere (lightcurve.py:99-254).  Triple lenses
+    (triple_routing): "contour" integrates every point, as the reference's mag()
+    (lightcurve.py:226-227); "reference" routes by the reference's triple
+    hexadecapole and triple proximity test as written (lightcurve.py:37-46,
+    third-lens terms at -r3), which accepts points where the hexadecapole is
+    tens of percent off; "corrected" uses the same test with the third lens at
+    r3, where the lens equation puts it."""
     wt, was_np = _to_device(w_points, torch.complex128)
     shape = wt.shape
     wf = wt.reshape(-1).contiguous()
@@ -322,7 +349,8 @@ def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, n
     out = torch.empty(n, dtype=torch.float64, device=wf.device)
     route = torch.empty(n, dtype=torch.uint8, device=wf.device)
     st = torch.zeros(n, dtype=torch.int32, device=wf.device)
-    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling)
+    opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling,
+                       triple_routing=triple_routing)
     with torch.cuda.device(wf.device):
         L.check(L.lib().cgb_mag(_ptr(wf), _ptr(out), _ptr(route), n, float(rho), L.lens_params(nlenses, params), opts,
                                 _ptr(st), _stream()), "cgb_mag")
@@ -352,8 +380,9 @@ def _batched_args(offsets, t, curves):
     return off.contiguous(), tt.contiguous(), cv.contiguous()
 
 
-def _workspace(n, device):
-    nbytes = int(L.lib().cgb_mag_lc_batched_workspace_bytes(n))
+def _workspace(n, device, vjp=False):
+    nbytes = int(L.lib().cgb_mag_lc_batched_vjp_workspace_bytes(n) if vjp else
+                 L.lib().cgb_mag_lc_batched_workspace_bytes(n))
     return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device), nbytes
 
 
@@ -400,7 +429,7 @@ def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=Fa
     mag_out = torch.empty(n, dtype=torch.float64, device=dev)
     route = torch.empty(n, dtype=torch.uint8, device=dev)
     grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
-    ws, nbytes = _workspace(n, dev)
+    ws, nbytes = _workspace(n, dev, vjp=True)
     opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
                        grad_fp64_above, labelling)
     with torch.cuda.device(dev):

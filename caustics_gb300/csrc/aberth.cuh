@@ -28,6 +28,7 @@
 #define CGB_ST_FALLBACK 4u   // mixed solver fell back to FP64 Aberth
 #define CGB_ST_MERGE 8u      // contour linking left open segments or overflowed its buffer
 #define CGB_ST_CAPACITY 16u  // limb / contour buffers too small for the request
+#define CGB_ST_INVALID 32u   // a non-finite or out-of-domain input: the item's output is NaN
 
 // real_guess: the reference's r*sin(phi) real initial guesses (init_est.h:95),
 // used only to reproduce the reference's labelling of roots.

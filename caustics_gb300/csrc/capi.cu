@@ -190,6 +190,13 @@ int cgb_ea_solve(const double *coeffs, const double *roots_init, double *roots, 
                      "cgb_ea_solve launch");
 }
 
+int cgb_lens_polynomial(const double *w, double *coeffs, int64_t n, cgb_lens_params lens, void *stream) {
+  if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
+  if (n > 0 && (!w || !coeffs)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!lens_ok(lens)) return fail(CGB_ERR_INVALID, "invalid lens parameters%s");
+  return cuda_status(launch_lens_poly(lens_of(lens), w, coeffs, n, (cudaStream_t)stream), "cgb_lens_polynomial launch");
+}
+
 int cgb_ea_roots_jvp(const double *coeffs, const double *roots, const double *dcoeffs, double *droots, int64_t n,
                      int32_t deg, void *stream) {
   if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
@@ -322,6 +329,11 @@ size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints) {
   return 16 + 16 * (size_t)(npoints > 0 ? npoints : 0);
 }
 static size_t batched_queue_bytes(int64_t npoints) { return 16 + 8 * (size_t)(npoints > 0 ? npoints : 0); }
+// The adjoint also keeps one cotangent-weighted gradient row (8 doubles) per
+// point, summed per curve in a fixed order afterwards.
+size_t cgb_mag_lc_batched_vjp_workspace_bytes(int64_t npoints) {
+  return cgb_mag_lc_batched_workspace_bytes(npoints) + 64 * (size_t)(npoints > 0 ? npoints : 0);
+}
 
 static int batched_setup(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
                          int64_t npoints, const cgb_es_options *opts, void *ws, size_t ws_bytes, EsParams &P) {
@@ -371,24 +383,29 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
                            uint32_t *status, const cgb_es_options *opts, void *workspace, size_t workspace_bytes,
                            void *stream) {
   if (!grad || (npoints > 0 && (!mag || !route || !cot))) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (!workspace || workspace_bytes < cgb_mag_lc_batched_vjp_workspace_bytes(npoints))
+    return fail(CGB_ERR_INVALID, "workspace too small (see cgb_mag_lc_batched_vjp_workspace_bytes)%s");
   EsParams P;
   int rc = batched_setup(offsets, t, curves, ncurves, npoints, opts, workspace, workspace_bytes, P);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  rc = cuda_status(cudaMemsetAsync(grad, 0, sizeof(double) * 8 * (size_t)ncurves, s), "gradient reset");
-  if (rc || npoints == 0) return rc;
+  if (npoints == 0)
+    return cuda_status(cudaMemsetAsync(grad, 0, sizeof(double) * 8 * (size_t)ncurves, s), "gradient reset");
   rc = cuda_status(cudaMemsetAsync(workspace, 0, 16, s), "queue reset");
   if (rc) return rc;
   P.cot = cot;
   P.cgrad = grad;
+  P.grow = reinterpret_cast<double *>((char *)workspace + cgb_mag_lc_batched_workspace_bytes(npoints));
   const int prec_ps = opts->precision == CGB_PREC_MIXED ? MIXED : FP64;
   rc = cuda_status(launch_lc_points_batched(P, npoints, mag, route, status, prec_ps,
                                             (unsigned long long *)workspace, (int64_t *)((char *)workspace + 16), true,
                                             s),
                    "cgb_mag_lc_batched_vjp point pass");
   if (rc) return rc;
-  return cuda_status(launch_es_grad(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
-                     "cgb_mag_lc_batched_vjp contour pass");
+  rc = cuda_status(launch_es_grad(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
+                   "cgb_mag_lc_batched_vjp contour pass");
+  if (rc) return rc;
+  return cuda_status(launch_curve_grad_reduce(offsets, ncurves, P.grow, grad, s), "cgb_mag_lc_batched_vjp curve sums");
 }
 
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
@@ -419,7 +436,10 @@ int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho,
   cudaStream_t s = (cudaStream_t)stream;
   const int prec = solver_precision(lens, opts->precision);
   const int prec_ps = point_source_precision(lens, prec) == CGB_PREC_MIXED ? MIXED : FP64;
-  rc = cuda_status(launch_lc_points(P.L, lens.q, w, rho, mag, route, n, P.itmax, prec_ps, status, s),
+  if (opts->triple_routing < 0 || opts->triple_routing > 2)
+    return fail(CGB_ERR_INVALID, "triple_routing must be 0, 1 or 2%s");
+  rc = cuda_status(launch_lc_points(P.L, lens.q, w, rho, mag, route, n, P.itmax, prec_ps, status,
+                                    opts->triple_routing, s),
                    "cgb_mag point pass launch");
   if (rc) return rc;
   int grid = opts->grid > 0 ? opts->grid : (int)((n < 8 * sm_count()) ? n : 8 * sm_count());
@@ -456,6 +476,14 @@ extern "C" int cgb_mag_lc_batched_noalloc(const int64_t *offsets, const double *
   if (rc) return rc;
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return fail(CGB_ERR_UNSUPPORTED, "cgb_mag_lc_batched_noalloc: device ordinal out of range%s");
+  if (stream) {  // the scratch is the current device's: the stream must be on it too
+    int sdev = -1;
+    rc = cuda_status(cudaStreamGetDevice((cudaStream_t)stream, &sdev), "cgb_mag_lc_batched_noalloc: stream device");
+    if (rc) return rc;
+    if (sdev != dev)
+      return fail(CGB_ERR_INVALID,
+                  "cgb_mag_lc_batched_noalloc: the stream belongs to another device than the current one%s");
+  }
   void *ws = nullptr;
   {
     // first call on a device: resolve the array's address in that device's context

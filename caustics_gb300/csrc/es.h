@@ -59,6 +59,7 @@ struct EsParams {
   // weighted sum per curve [ncurves][8] of (s, q, rho, u1, u0, alpha, t0, tE)
   double *gout;
   const double *cot;
+  double *grow;   // batched adjoint: cotangent-weighted gradient row [npoints][8] per point
   double *cgrad;
   double s_user, q_user;  // single-lens parameters (for the adjoint's chain rule)
   double *dbg;  // optional per-point diagnostics (cgb_debug_extended_source), stride ES_DBG_STRIDE(Lcap)
@@ -90,6 +91,11 @@ cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t 
 // cotangent-weighted gradient to P.cgrad.
 cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
                                      int precision, unsigned long long *qcount, int64_t *qlist, bool grad,
+                                     cudaStream_t stream);
+
+// Per-curve sums of the batched adjoint's point rows: cgrad[c][k] = sum over
+// offsets[c] <= i < offsets[c+1] of grow[i][k], in a fixed order (deterministic).
+cudaError_t launch_curve_grad_reduce(const int64_t *offsets, int64_t ncurves, const double *grow, double *cgrad,
                                      cudaStream_t stream);
 
 // Gauss-Legendre nodes/weights on [-1, 1], ascending (host)

@@ -178,6 +178,24 @@ static __device__ int block_exclusive_scan(int *buf, int n, int *warp_tot) {
   return carry;
 }
 
+// Deterministic accumulation of per-lane values into per-key slots: acc[key]
+// += v for every lane with key >= 0, where the keys of a warp's lanes form
+// contiguous runs (a contour's points are consecutive).  Each run is summed by
+// a fixed shuffle tree and its first lane adds the total (one writer per run;
+// the runs of one warp have distinct keys, and a warp's calls follow program
+// order), so the result does not depend on scheduling.  All 32 lanes call.
+__device__ __forceinline__ void warp_run_add(int key, double v, double *acc, int stride = 1) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double u = __shfl_down_sync(0xffffffffu, v, o);
+    const int ku = __shfl_down_sync(0xffffffffu, key, o);
+    if (lane + o < 32 && ku == key) v += u;
+  }
+  const int kp = __shfl_up_sync(0xffffffffu, key, 1);
+  if (key >= 0 && (lane == 0 || kp != key)) acc[key * stride] += v;
+}
+
 // Length of the limb interval between slots s1 and s2 for the refinement
 // (extended_source.py:110-113): the largest |z2 - z1| over the rows that are a
 // real image at either end, taken as sqrt of the largest squared distance
@@ -977,10 +995,11 @@ __device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th,
 template <int NL, int PREC>
 __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsItem &I, int ncont, int ntot,
                             const int *cstart, const int *cpar, const cd *centroid,
-                            double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2], double *pgr,
-                            double *tot_sh, int64_t pi, double *mag, const float (*glf)[2][GL_MAX]) {
+                            double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2],
+                            double (*cgr_w)[MAX_CLOSED + N_CONTOURS][2], double (*pgr_w)[6], double *tot_sh,
+                            int64_t pi, double *mag, const float (*glf)[2][GL_MAX]) {
   constexpr int DEG = NL * NL + 1;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     double tot = 0.0;
     for (int c = 0; c < ncont; ++c) {
@@ -992,58 +1011,71 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
   }
   for (int i = tid; i < ntot; i += ES_THREADS) S.GG[i] = mk(0, 0);
   __syncthreads();
-  // pass 2: node-level derivatives, trapezoid weights, centroids, direct terms
+  // pass 2: node-level derivatives, trapezoid weights, centroids, direct terms.
+  // Sums over points run in a fixed order (per-thread partials, shuffle trees,
+  // per-warp slots summed in warp order): two identical calls give identical bits.
   double acc[6] = {0, 0, 0, 0, 0, 0};
   {
     int c = 0;
-    for (int i = tid; i < ntot; i += ES_THREADS) {
-      while (i >= cstart[c + 1]) ++c;
-      const int b = cstart[c], e = min(cstart[c + 1], ntot);
-      const double pc = cpar[c];
-      const int ip = i > b ? i - 1 : i, in = i + 1 < e ? i + 1 : i;
-      const cd zc = S.Z[S.CP[i]], zp = S.Z[S.CP[ip]], zn = S.Z[S.CP[in]];
+    for (int base = warp * 32; base < ntot; base += ES_THREADS) {  // warp-uniform trip count
+      const int i = base + lane;
+      double cg0 = 0.0, cg1 = 0.0;  // this point's d T / d(x0_c, y0_c)
+      int key = -1;
+      if (i < ntot) {
+        while (i >= cstart[c + 1]) ++c;
+        key = c;
+        const int b = cstart[c], e = min(cstart[c + 1], ntot);
+        const double pc = cpar[c];
+        const int ip = i > b ? i - 1 : i, in = i + 1 < e ? i + 1 : i;
+        const cd zc = S.Z[S.CP[i]], zp = S.Z[S.CP[ip]], zn = S.Z[S.CP[in]];
+        if (P.ld) {
+          const double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
+          // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2, so P_i wx_i + Q_i wy_i
+          // contributes P_i (t_in - t_ip).x / 2 + Q_i (t_in - t_ip).y / 2 per
+          // parameter.  Summed by parts against the FP64 image tangents rather than
+          // scattered into the neighbours' position adjoints, where it would become
+          // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
+          // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
+          cd tn[6], tp[6], ti[6];
+          const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
+          image_tangents(I, zn, S.TH[cpn / DEG], tn);
+          image_tangents(I, zp, S.TH[cpp / DEG], tp);
+          image_tangents(I, zc, S.TH[S.CP[i] / DEG], ti);
+          // Near a critical curve the tangents grow like 1/|det J| and the
+          // pointwise contributions cancel in the sum; there the FP32 node values
+          // (relative error ~1e-7) would be amplified, so such points run the
+          // quadrature in FP64.
+          double amp2 = 0.0;
+  #pragma unroll
+          for (int k = 0; k < 6; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
+          PQGrad g;
+          if (PREC == MIXED && amp2 <= P.grad_amp2)
+            ld_pq_grad<float, cf>(P, I, zc, centroid[c], g, glf);
+          else
+            ld_pq_grad<double, cd>(P, I, zc, centroid[c], g, glf);
+          const cd pq = mk(g.P, g.Q);
+          atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
+          atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
+  #pragma unroll
+          for (int k = 0; k < 6; ++k)
+            acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
+          cg1 = pc * wx * g.Pa;
+          cg0 = pc * wy * g.Qa;
+  #pragma unroll
+          for (int k = 0; k < 6; ++k) acc[k] += pc * (wx * g.Pk[k] + wy * g.Qk[k]);
+        } else if (i + 1 < e) {
+          // pair (i, i+1): 1/4 [(x_i + x_{i+1})(y_{i+1} - y_i) - (y_i + y_{i+1})(x_{i+1} - x_i)];
+          // each GG entry receives exactly two addends onto zero, an order-free sum
+          const cd a = zc, q = zn;
+          atomicAdd(&S.GG[i].x, pc * 0.5 * q.y);
+          atomicAdd(&S.GG[i].y, -pc * 0.5 * q.x);
+          atomicAdd(&S.GG[i + 1].x, -pc * 0.5 * a.y);
+          atomicAdd(&S.GG[i + 1].y, pc * 0.5 * a.x);
+        }
+      }
       if (P.ld) {
-        const double wx = 0.5 * (zn.x - zp.x), wy = 0.5 * (zn.y - zp.y);
-        // wx_i = (x_in - x_ip)/2, wy_i = (y_in - y_ip)/2, so P_i wx_i + Q_i wy_i
-        // contributes P_i (t_in - t_ip).x / 2 + Q_i (t_in - t_ip).y / 2 per
-        // parameter.  Summed by parts against the FP64 image tangents rather than
-        // scattered into the neighbours' position adjoints, where it would become
-        // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
-        // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
-        cd tn[6], tp[6], ti[6];
-        const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
-        image_tangents(I, zn, S.TH[cpn / DEG], tn);
-        image_tangents(I, zp, S.TH[cpp / DEG], tp);
-        image_tangents(I, zc, S.TH[S.CP[i] / DEG], ti);
-        // Near a critical curve the tangents grow like 1/|det J| and the
-        // pointwise contributions cancel in the sum; there the FP32 node values
-        // (relative error ~1e-7) would be amplified, so such points run the
-        // quadrature in FP64.
-        double amp2 = 0.0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
-        PQGrad g;
-        if (PREC == MIXED && amp2 <= P.grad_amp2)
-          ld_pq_grad<float, cf>(P, I, zc, centroid[c], g, glf);
-        else
-          ld_pq_grad<double, cd>(P, I, zc, centroid[c], g, glf);
-        const cd pq = mk(g.P, g.Q);
-        atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
-        atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-          acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
-        atomicAdd(&cgr[c][1], pc * wx * g.Pa);
-        atomicAdd(&cgr[c][0], pc * wy * g.Qa);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) acc[k] += pc * (wx * g.Pk[k] + wy * g.Qk[k]);
-      } else if (i + 1 < e) {
-        // pair (i, i+1): 1/4 [(x_i + x_{i+1})(y_{i+1} - y_i) - (y_i + y_{i+1})(x_{i+1} - x_i)]
-        const cd a = zc, q = zn;
-        atomicAdd(&S.GG[i].x, pc * 0.5 * q.y);
-        atomicAdd(&S.GG[i].y, -pc * 0.5 * q.x);
-        atomicAdd(&S.GG[i + 1].x, -pc * 0.5 * a.y);
-        atomicAdd(&S.GG[i + 1].y, pc * 0.5 * a.x);
+        warp_run_add(key, cg0, &cgr_w[warp][0][0], 2);
+        warp_run_add(key, cg1, &cgr_w[warp][0][1], 2);
       }
     }
   }
@@ -1052,8 +1084,14 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     double v = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((tid & 31) == 0 && v != 0.0) atomicAdd(&pgr[k], v);
+    if (lane == 0) pgr_w[warp][k] += v;
     acc[k] = 0.0;
+  }
+  __syncthreads();
+  for (int q = tid; q < 2 * ncont; q += ES_THREADS) {  // per-contour sums in warp order
+    double v = 0.0;
+    for (int w = 0; w < ES_WARPS; ++w) v += cgr_w[w][q >> 1][q & 1];
+    cgr[q >> 1][q & 1] = v;
   }
   __syncthreads();
   // pass 3: every contour point's image through the lens equation:
@@ -1080,7 +1118,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     double v = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((tid & 31) == 0 && v != 0.0) atomicAdd(&pgr[k], v);
+    if (lane == 0) pgr_w[warp][k] += v;
   }
   __syncthreads();
   if (tid == 0) {
@@ -1088,14 +1126,18 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     const double mu = fabs(tot) / (3.14159265358979323846 * rho * rho);
     const double sT = (tot > 0 ? 1.0 : (tot < 0 ? -1.0 : 0.0)) / (3.14159265358979323846 * rho * rho);
     double d[6];
-    for (int k = 0; k < 6; ++k) d[k] = sT * pgr[k];
+    for (int k = 0; k < 6; ++k) {
+      double v = 0.0;
+      for (int w = 0; w < ES_WARPS; ++w) v += pgr_w[w][k];
+      d[k] = sT * v;
+    }
     d[GK_RHO] -= 2.0 * mu / rho;
     // (a, e1, x_cm) -> (s, q): a = s/2, e1 = 1/(1+q), x_cm = a(1-q)/(1+q)
     const double q = I.q, a = 0.5 * I.s, opq = 1.0 + q;
     const double ds = 0.5 * d[GK_A] + d[GK_WX] * (1.0 - q) / (2.0 * opq);
     const double dq = -d[GK_E1] / (opq * opq) - d[GK_WX] * 2.0 * a / (opq * opq);
     mag[pi] = mu;
-    if (I.curve >= 0 && P.cgrad) {
+    if (I.curve >= 0 && P.grow) {
       const CurveDev cv = P.curves[I.curve];
       const double ct = P.cot ? P.cot[pi] : 1.0;
       double sa, ca;
@@ -1106,15 +1148,17 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
       const double dal = d[GK_WX] * (-cv.u0 * sa + tau * ca) + d[GK_WY] * (-cv.u0 * ca - tau * sa);
       const double dt0 = -(d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
       const double dtE = -tau * (d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
-      double *gp = P.cgrad + I.curve * 8;
-      atomicAdd(gp + 0, ct * ds);
-      atomicAdd(gp + 1, ct * dq);
-      atomicAdd(gp + 2, ct * d[GK_RHO]);
-      atomicAdd(gp + 3, ct * d[GK_U1]);
-      atomicAdd(gp + 4, ct * du0);
-      atomicAdd(gp + 5, ct * dal);
-      atomicAdd(gp + 6, ct * dt0);
-      atomicAdd(gp + 7, ct * dtE);
+      // this point's cotangent-weighted row; curve_grad_reduce_kernel sums the
+      // rows of each curve in a fixed order
+      double *gp = P.grow + pi * 8;
+      gp[0] = ct * ds;
+      gp[1] = ct * dq;
+      gp[2] = ct * d[GK_RHO];
+      gp[3] = ct * d[GK_U1];
+      gp[4] = ct * du0;
+      gp[5] = ct * dal;
+      gp[6] = ct * dt0;
+      gp[7] = ct * dtE;
     } else if (P.gout) {
       double *gp = P.gout + pi * 6;
       gp[0] = ds;
@@ -1237,7 +1281,10 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
   __shared__ int64_t item_sh, iord_sh;  // point index, item ordinal
   __shared__ EsItem item;
   __shared__ double cgr[MAX_CLOSED + N_CONTOURS][2];  // adjoint: dT/dx0_c, dT/dy0_c
-  __shared__ double pgr[6];                          // adjoint: direct dT/d(rho, u1, w0x, w0y, a, e1)
+  // adjoint partial sums per warp (summed in warp order): dT/d(x0_c, y0_c) and
+  // the direct dT/d(rho, u1, w0x, w0y, a, e1)
+  __shared__ double cgr_w[GRAD ? ES_WARPS : 1][MAX_CLOSED + N_CONTOURS][2];
+  __shared__ double pgr_w[GRAD ? ES_WARPS : 1][6];
   __shared__ double tot_sh;
   __shared__ float glf[2][2][GL_MAX];  // FP32 Gauss-Legendre tables [half][nodes | weights][j]
   for (int i = threadIdx.x; i < 2 * GL_MAX; i += ES_THREADS) {
@@ -1325,6 +1372,17 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
     uint32_t flags = 0;
     __syncthreads();
     const EsItem &I = item;
+    if (!isfinite(I.w0.x) || !isfinite(I.w0.y)) {  // a non-finite source centre (CTA-uniform): not evaluated
+      if (tid == 0) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        mag[pi] = nan;
+        if (status) status[pi] = route ? (status[pi] | CGB_ST_INVALID) : CGB_ST_INVALID;
+        if (GRAD && P.gout)
+          for (int k = 0; k < 6; ++k) P.gout[pi * 6 + k] = nan;
+      }
+      __syncthreads();
+      continue;
+    }
     if (P.dbg && tid == 0) {
       clk[0] = clock64();
       for (int c = 0; c < 7; ++c) dbg_ref[c] = 0;
@@ -2116,10 +2174,13 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
 
     // ---- F: integrals ----
     for (int c = tid; c < MAX_CLOSED + N_CONTOURS; c += ES_THREADS) {
-      for (int w = 0; w < ES_WARPS; ++w) contour_acc[w][c] = 0.0;
+      for (int w = 0; w < ES_WARPS; ++w) {
+        contour_acc[w][c] = 0.0;
+        if (GRAD) cgr_w[w][c][0] = cgr_w[w][c][1] = 0.0;
+      }
       cgr[c][0] = cgr[c][1] = 0.0;
     }
-    if (tid < 6) pgr[tid] = 0.0;
+    if (GRAD && tid < 6 * ES_WARPS) pgr_w[tid / 6][tid % 6] = 0.0;
     if (P.ld) {
       // centroids (sum over all points incl. the closing point) / count
       for (int c = warp; c < ncont; c += ES_WARPS) {
@@ -2161,25 +2222,31 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
           pq.x += __shfl_xor_sync(0xffffffffu, pq.x, o);
           pq.y += __shfl_xor_sync(0xffffffffu, pq.y, o);
         }
-        if (valid && r == 0) {
-          atomicAdd(&contour_acc[warp][c], pq.x * wx + pq.y * wy);
-        }
+        warp_run_add(valid ? c : -1, (valid && r == 0) ? pq.x * wx + pq.y * wy : 0.0, contour_acc[warp]);
       }
     } else {
       // uniform: 1/2 sum (x_i + x_{i+1})/2 (y_{i+1} - y_i) - (y_i + y_{i+1})/2 (x_{i+1} - x_i)
       int c = 0;
-      for (int i = tid; i < ntot; i += ES_THREADS) {
-        while (i >= cstart[c + 1]) ++c;
-        const int e = min(cstart[c + 1], ntot);
-        if (i + 1 >= e) continue;
-        cd a = S.Z[S.CP[i]], bq = S.Z[S.CP[i + 1]];
-        double v = 0.25 * ((a.x + bq.x) * (bq.y - a.y) - (a.y + bq.y) * (bq.x - a.x));
-        atomicAdd(&contour_acc[warp][c], v);
+      for (int base = warp * 32; base < ntot; base += ES_THREADS) {  // warp-uniform trip count
+        const int i = base + lane;
+        double v = 0.0;
+        int key = -1;
+        if (i < ntot) {
+          while (i >= cstart[c + 1]) ++c;
+          key = c;
+          const int e = min(cstart[c + 1], ntot);
+          if (i + 1 < e) {
+            const cd a = S.Z[S.CP[i]], bq = S.Z[S.CP[i + 1]];
+            v = 0.25 * ((a.x + bq.x) * (bq.y - a.y) - (a.y + bq.y) * (bq.x - a.x));
+          }
+        }
+        warp_run_add(key, v, contour_acc[warp]);
       }
     }
     __syncthreads();
     if (GRAD)
-      es_backward<NL, PREC>(P, S, I, ncont, ntot, cstart, cpar, centroid, contour_acc, cgr, pgr, &tot_sh, pi, mag, glf);
+      es_backward<NL, PREC>(P, S, I, ncont, ntot, cstart, cpar, centroid, contour_acc, cgr, cgr_w, pgr_w, &tot_sh, pi,
+                            mag, glf);
     if (tid == 0 && !GRAD) {
       double tot = 0.0;
       double *dbg = P.dbg ? P.dbg + (size_t)pi * ES_DBG_STRIDE(P.Lcap) : nullptr;

@@ -272,6 +272,55 @@ __device__ __forceinline__ bool proximity_test_binary(const Lens &L, cd w, const
   return t_f && t_mc;
 }
 
+// Triple-lens proximity test (the nlenses == 3 branch of lightcurve.py:23-75),
+// same constants and structure as the binary one over the 10 images.
+// as_written: the reference's f, f', f'' as it writes them (third-lens terms
+// at -r3, f'' third term e3/(z+r3)^3); otherwise the third lens at r3 (where
+// the lens equation and the hexadecapole put it) and f'' = -2 sum_j eps_j /
+// (z - r_j)^3.
+__device__ __forceinline__ bool proximity_test_triple(const Lens &L, cd w, const cd (&z)[10], uint32_t mask,
+                                                      double rho, double delta_mu, bool as_written) {
+  const double a = L.r[0].x, e1 = L.eps[0], e2 = L.eps[1], e3 = L.eps[2];
+  const cd r3 = as_written ? mk(-L.r[2].x, -L.r[2].y) : L.r[2];  // the test's third-lens position
+  const double c3 = as_written ? 1.0 : -2.0;                      // its f'' coefficient
+  const double c_m = 1e-2, gam = 0.02, c_f = 4.0, rho_min = 1e-3;
+  auto f = [&](cd u) {
+    return (crecip(u - mk(a, 0)) * e1 + crecip(u + mk(a, 0)) * e2 + crecip(u - r3) * e3) * -1.0;
+  };
+  auto fp = [&](cd u) {
+    cd p = crecip(u - mk(a, 0)), m = crecip(u + mk(a, 0)), t = crecip(u - r3);
+    return p * p * e1 + m * m * e2 + t * t * e3;
+  };
+  auto fpp = [&](cd u) {
+    cd p = crecip(mk(a, 0) - u), m = crecip(mk(a, 0) + u), t = crecip(u - r3);
+    return (p * p * p * e1 - m * m * m * e2) * 2.0 + t * t * t * (c3 * e3);
+  };
+  double cusp = 0.0, fac = 0.0;
+  int nfalse = 0;
+  const double rr = (rho + rho_min) * (rho + rho_min);
+#pragma unroll 1
+  for (int i = 0; i < 10; ++i) {
+    cd zb = conj(z[i]);
+    cd zh = conj(w) - f(z[i]);
+    cd fpz = fp(z[i]), fppz = fpp(z[i]), fpzb = fp(zb), fpzh = fp(zh), fppzb = fpp(zb);
+    double J = 1.0 - cabs(fpz * fpzb);
+    bool real = (mask >> i) & 1u;
+    if (real) {
+      cd t = fpzb * fpzb * fpzb * fppz * fppz * 3.0;
+      double J5 = J * J * J * J * J;
+      cusp += fabs(6.0 * t.y / J5 * rr);
+    } else {
+      ++nfalse;
+      double Jh = 1.0 - cabs(fpz * fpzh);
+      cd den = fppzb * fpz * Jh - fppz * fpzb * fpzh * Jh;
+      fac += cabs(cdiv(mk(J * Jh * Jh, 0), den));
+    }
+  }
+  bool t_mc = gam * cusp + delta_mu < c_m;
+  bool t_f = (nfalse == 0) ? true : (0.5 * fac > c_f * (rho + rho_min));
+  return t_f && t_mc;
+}
+
 // lightcurve.py:78-85, with q' = e1/(1-e1) (the inverse of q, as in the reference)
 __device__ __forceinline__ bool planetary_test(const Lens &L, cd w, double rho) {
   const double a = L.r[0].x, e1 = L.eps[0];

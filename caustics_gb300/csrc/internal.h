@@ -9,6 +9,9 @@ namespace cgb {
 
 enum Precision : int { FP64 = 0, MIXED = 1, FP64_COMP = 2 };
 
+// lens-equation polynomial coefficients, low -> high (point_source.cu)
+cudaError_t launch_lens_poly(const Lens &L, const double *w, double *coeffs, int64_t n, cudaStream_t stream);
+
 cudaError_t launch_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int deg,
                             int itmax, int precision, uint32_t *status, cudaStream_t stream);
 
@@ -40,6 +43,7 @@ cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *i
 // q < 0.01) tests.  Writes mu_multi (the hexadecapole magnification) into mag and
 // route[i] = 1 where the full contour integration is needed.
 cudaError_t launch_lc_points(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
-                             int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream);
+                             int64_t n, int itmax, int precision, uint32_t *status, int triple_routing,
+                             cudaStream_t stream);
 
 }  // namespace cgb

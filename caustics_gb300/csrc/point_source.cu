@@ -1,6 +1,8 @@
 // Host launchers of the point-source kernels (point_source.cuh): select the
 // per-precision instantiation (ps_fp64.cu, ps_mixed.cu, ps_comp.cu) from the
 // runtime precision.  The light-curve point passes only take FP64 or MIXED.
+// Also two precision-free kernels: the lens-equation polynomial of source
+// positions, and the per-curve sums of the batched adjoint's point rows.
 #include "es.h"
 #include "internal.h"
 
@@ -14,10 +16,78 @@ cudaError_t launch_mag_ps_p(const Lens &L, const double *w, double *mag, double 
                             int64_t n, int itmax, uint32_t *status, cudaStream_t stream);
 template <int PREC>
 cudaError_t launch_lc_points_p(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
-                               int64_t n, int itmax, uint32_t *status, cudaStream_t stream);
+                               int64_t n, int itmax, uint32_t *status, int triple_routing, cudaStream_t stream);
 template <int PREC>
 cudaError_t launch_lc_points_batched_p(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
                                        unsigned long long *qcount, int64_t *qlist, bool grad, cudaStream_t stream);
+
+constexpr int AUX_THREADS = 128;
+
+// cgrad[c][k] = sum of the rows grow[i][k] of curve c's points: one warp per
+// curve, each lane summing a fixed stride of points, then a fixed shuffle tree,
+// so repeated calls give identical bits.
+__global__ void __launch_bounds__(AUX_THREADS)
+    curve_grad_reduce_kernel(const int64_t *__restrict__ offsets, int64_t ncurves, const double *__restrict__ grow,
+                             double *__restrict__ cgrad) {
+  const int64_t c = (int64_t)blockIdx.x * (AUX_THREADS / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= ncurves) return;
+  const int64_t b = offsets[c], e = offsets[c + 1];
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int64_t i = b + lane; i < e; i += 32) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] += grow[i * 8 + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+  }
+  if (lane < 8) {
+    double v = acc[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) v = lane == k ? acc[k] : v;
+    cgrad[c * 8 + lane] = v;
+  }
+}
+
+cudaError_t launch_curve_grad_reduce(const int64_t *offsets, int64_t ncurves, const double *grow, double *cgrad,
+                                     cudaStream_t stream) {
+  if (ncurves == 0) return cudaSuccess;
+  constexpr int per_block = AUX_THREADS / 32;
+  curve_grad_reduce_kernel<<<(unsigned)((ncurves + per_block - 1) / per_block), AUX_THREADS, 0, stream>>>(
+      offsets, ncurves, grow, cgrad);
+  return cudaGetLastError();
+}
+
+// Lens-equation polynomial of each source position (user frame; shifted by
+// x_cm as mag_point_source does), low -> high: one thread per position.
+template <int NL>
+__global__ void __launch_bounds__(AUX_THREADS) lens_poly_kernel(Lens L, const cd *__restrict__ w,
+                                                                cd *__restrict__ coeffs, int64_t n) {
+  constexpr int DEG = NL * NL + 1;
+  const int64_t i = (int64_t)blockIdx.x * AUX_THREADS + threadIdx.x;
+  if (i >= n) return;
+  const cd wi = mk(w[i].x + L.x_cm, w[i].y);
+  cd p[DEG + 1];
+  lens_poly<NL>(L, wi, p);
+#pragma unroll
+  for (int k = 0; k <= DEG; ++k) coeffs[i * (DEG + 1) + k] = p[k];
+}
+
+cudaError_t launch_lens_poly(const Lens &L, const double *w, double *coeffs, int64_t n, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((n + AUX_THREADS - 1) / AUX_THREADS);
+  const cd *wc = reinterpret_cast<const cd *>(w);
+  cd *c = reinterpret_cast<cd *>(coeffs);
+  if (L.n == 2)
+    lens_poly_kernel<2><<<grid, AUX_THREADS, 0, stream>>>(L, wc, c, n);
+  else if (L.n == 3)
+    lens_poly_kernel<3><<<grid, AUX_THREADS, 0, stream>>>(L, wc, c, n);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int deg,
                             int itmax, int precision, uint32_t *status, cudaStream_t stream) {
@@ -40,10 +110,11 @@ cudaError_t launch_mag_ps(const Lens &L, const double *w, double *mag, double *i
 }
 
 cudaError_t launch_lc_points(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
-                             int64_t n, int itmax, int precision, uint32_t *status, cudaStream_t stream) {
+                             int64_t n, int itmax, int precision, uint32_t *status, int triple_routing,
+                             cudaStream_t stream) {
   switch (precision) {
-    case FP64: return launch_lc_points_p<FP64>(L, q, w, rho, mag, route, n, itmax, status, stream);
-    case MIXED: return launch_lc_points_p<MIXED>(L, q, w, rho, mag, route, n, itmax, status, stream);
+    case FP64: return launch_lc_points_p<FP64>(L, q, w, rho, mag, route, n, itmax, status, triple_routing, stream);
+    case MIXED: return launch_lc_points_p<MIXED>(L, q, w, rho, mag, route, n, itmax, status, triple_routing, stream);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -59,8 +59,18 @@ __global__ void __launch_bounds__(PS_THREADS) ea_solve_kernel(const cd *__restri
   }
   uint32_t flags = 0;
   if (active) {
-    int it = solve<PREC, DEG>(p, z, itmax, roots_init != nullptr, flags);
-    if (it < 0) flags |= CGB_ST_NOCONV;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k <= DEG; ++k) finite &= isfinite(p[k].x) && isfinite(p[k].y);
+    if (finite) {
+      int it = solve<PREC, DEG>(p, z, itmax, roots_init != nullptr, flags);
+      if (it < 0) flags |= CGB_ST_NOCONV;
+    } else {  // not solved: NaN roots
+      flags = CGB_ST_INVALID;
+      const double nan = __longlong_as_double(0x7ff8000000000000ll);
+#pragma unroll
+      for (int k = 0; k < DEG; ++k) z[k] = mk(nan, nan);
+    }
 #pragma unroll
     for (int k = 0; k < DEG; ++k) stage[tid * DEG + k] = z[k];
     if (status) status[base + tid] = flags;
@@ -121,12 +131,19 @@ __global__ void __launch_bounds__(PS_THREADS) mag_ps_kernel(Lens L, const cd *__
   uint32_t flags = 0, m = 0;
   if (i < n) {
     cd wi = w[i];
-    wi.x += L.x_cm;
-    m = images<PREC, NL>(L, wi, z, itmax, flags);
     double mu = 0.0;
+    if (isfinite(wi.x) && isfinite(wi.y)) {
+      wi.x += L.x_cm;
+      m = images<PREC, NL>(L, wi, z, itmax, flags);
 #pragma unroll
-    for (int k = 0; k < DEG; ++k)
-      if ((m >> k) & 1u) mu += 1.0 / fabs(lens_det<NL>(L, z[k]));
+      for (int k = 0; k < DEG; ++k)
+        if ((m >> k) & 1u) mu += 1.0 / fabs(lens_det<NL>(L, z[k]));
+    } else {  // not solved: NaN magnification and images
+      flags = CGB_ST_INVALID;
+      mu = __longlong_as_double(0x7ff8000000000000ll);
+#pragma unroll
+      for (int k = 0; k < DEG; ++k) z[k] = mk(mu, mu);
+    }
     mag[i] = mu;
     if (status) status[i] = flags;
     if (mask_out) mask_out[i] = m;
@@ -157,25 +174,34 @@ cudaError_t launch_mag_ps_p(const Lens &L, const double *w, double *mag, double 
   return cudaGetLastError();
 }
 
-// Per-point pass of mag(): binary lenses get the hexadecapole magnification and
-// the routing test; triple lenses always route to the contour integral
-// (lightcurve.py:226-227).
+// Per-point pass of mag(): the hexadecapole magnification and the routing
+// test for binary lenses; triple lenses route to the contour integral
+// (lightcurve.py:226-227) unless triple_routing asks for the reference's
+// triple hexadecapole with its triple proximity test (1: as written, 2: third
+// lens at r3).  A non-finite source position gives NaN and CGB_ST_INVALID.
 template <int PREC, int NL>
 __global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q, const cd *__restrict__ w, double rho,
                                                                double *__restrict__ mag, uint8_t *__restrict__ route,
-                                                               int64_t n, int itmax, uint32_t *__restrict__ status) {
+                                                               int64_t n, int itmax, uint32_t *__restrict__ status,
+                                                               int triple_routing) {
   constexpr int DEG = NL * NL + 1;
   const int64_t i = (int64_t)blockIdx.x * PS_THREADS + threadIdx.x;
   if (i >= n) return;
   uint32_t flags = 0;
   cd wi = w[i];
+  if (!isfinite(wi.x) || !isfinite(wi.y)) {
+    mag[i] = __longlong_as_double(0x7ff8000000000000ll);
+    route[i] = 0;
+    if (status) status[i] = CGB_ST_INVALID;
+    return;
+  }
   wi.x += L.x_cm;
-  // Triple lenses always take the contour integral (lightcurve.py:226-227); for
-  // q < 0.01 the routing test is proximity & planetary (lightcurve.py:216-224),
-  // so where the planetary test fails the point takes the contour integral
-  // whatever its images give: neither the images nor the hexadecapole are
-  // needed (the contour kernel writes mag).
-  if (NL != 2 || (q < 0.01 && !planetary_test(L, wi, rho))) {
+  // Triple lenses take the contour integral (lightcurve.py:226-227) unless
+  // routed; for q < 0.01 the routing test is proximity & planetary
+  // (lightcurve.py:216-224), so where the planetary test fails the point takes
+  // the contour integral whatever its images give: neither the images nor the
+  // hexadecapole are needed (the contour kernel writes mag).
+  if ((NL == 3 && triple_routing == 0) || (NL == 2 && q < 0.01 && !planetary_test(L, wi, rho))) {
     mag[i] = 0.0;
     route[i] = 1;
     if (status) status[i] = 0;
@@ -184,21 +210,21 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q,
   cd z[DEG];
   uint32_t m = images<PREC, NL>(L, wi, z, itmax, flags);
   double mu_multi = 0.0, dmu = 0.0;
-  bool hex_ok = false;
-  if (NL == 2) {
-#pragma unroll
-    for (int k = 0; k < DEG; ++k) {
-      if (!((m >> k) & 1u)) continue;
-      cd W[5];
-      hexa::wk<NL>(L, z[k], W);
-      double mu0, dq, dh;
-      hexa::terms(W, rho, 0.0, mu0, dq, dh);
-      mu_multi += fabs(mu0 + dq + dh);
-      dmu += fabs(dq) + fabs(dh);
-    }
-    const cd(&z5)[5] = reinterpret_cast<const cd(&)[5]>(z);
-    hex_ok = proximity_test_binary(L, wi, z5, m, rho, dmu);
-    // (q < 0.01: the planetary test passed above)
+#pragma unroll 1
+  for (int k = 0; k < DEG; ++k) {
+    if (!((m >> k) & 1u)) continue;
+    cd W[5];
+    hexa::wk<NL>(L, z[k], W);
+    double mu0, dq, dh;
+    hexa::terms(W, rho, 0.0, mu0, dq, dh);  // mag() passes no u1 (lightcurve.py:215)
+    mu_multi += fabs(mu0 + dq + dh);
+    dmu += fabs(dq) + fabs(dh);
+  }
+  bool hex_ok;
+  if constexpr (NL == 2) {
+    hex_ok = proximity_test_binary(L, wi, z, m, rho, dmu);  // (q < 0.01: the planetary test passed above)
+  } else {
+    hex_ok = proximity_test_triple(L, wi, z, m, rho, dmu, triple_routing == 1);
   }
   mag[i] = mu_multi;
   route[i] = hex_ok ? 0 : 1;
@@ -207,14 +233,15 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_kernel(Lens L, double q,
 
 template <int PREC>
 cudaError_t launch_lc_points_p(const Lens &L, double q, const double *w, double rho, double *mag, uint8_t *route,
-                               int64_t n, int itmax, uint32_t *status, cudaStream_t stream) {
+                               int64_t n, int itmax, uint32_t *status, int triple_routing, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
   const cd *wc = reinterpret_cast<const cd *>(w);
   if (L.n == 2)
-    lc_points_kernel<PREC, 2><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, status);
+    lc_points_kernel<PREC, 2><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, status, 0);
   else if (L.n == 3)
-    lc_points_kernel<PREC, 3><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, status);
+    lc_points_kernel<PREC, 3><<<grid, PS_THREADS, 0, stream>>>(L, q, wc, rho, mag, route, n, itmax, status,
+                                                               triple_routing);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
@@ -235,18 +262,32 @@ __device__ __forceinline__ int64_t curve_of(const int64_t *offsets, int64_t ncur
 
 // Per-point pass of batched mag(): images, hexadecapole, routing tests; points
 // that need the contour integral are appended to the device work queue
-// (qcount, qlist).  With GRAD, hexadecapole-routed points also add their
-// cotangent-weighted gradient to cgrad[curve][(s, q, rho, u1, u0, alpha, t0, tE)]
-// (forward-mode tangents through the images and the multipole series).
+// (qcount, qlist).  With GRAD, hexadecapole-routed points also write their
+// cotangent-weighted gradient row grow[i][(s, q, rho, u1, u0, alpha, t0, tE)]
+// (forward-mode tangents through the images and the multipole series); the
+// contour kernel writes the rows of the queued points.  Curves with parameters
+// out of the domain give NaN, CGB_ST_INVALID and a zero row.
 template <int PREC, bool GRAD>
 __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
     const CurveDev *__restrict__ curves, const int64_t *__restrict__ offsets, const double *__restrict__ times,
     int64_t ncurves, int64_t n, double *__restrict__ mag, uint8_t *__restrict__ route, uint32_t *__restrict__ status,
-    int itmax, unsigned long long *qcount, int64_t *qlist, const double *__restrict__ cot, double *cgrad) {
+    int itmax, unsigned long long *qcount, int64_t *qlist, const double *__restrict__ cot, double *grow) {
   const int64_t i = (int64_t)blockIdx.x * PS_THREADS + threadIdx.x;
   if (i >= n) return;
   const int64_t c = curve_of(offsets, ncurves, i);
   const CurveDev cv = curves[c];
+  if (!(cv.s > 0) || !(cv.q > 0) || !(cv.rho > 0) || !(cv.tE != 0) || !isfinite(cv.s) || !isfinite(cv.q) ||
+      !isfinite(cv.rho) || !isfinite(cv.u1) || !isfinite(cv.u0) || !isfinite(cv.alpha) || !isfinite(cv.t0) ||
+      !isfinite(cv.tE) || !isfinite(times[i])) {  // not evaluated: NaN, no gradient
+    mag[i] = __longlong_as_double(0x7ff8000000000000ll);
+    route[i] = 0;
+    if (status) status[i] = CGB_ST_INVALID;
+    if (GRAD) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) grow[i * 8 + k] = 0.0;
+    }
+    return;
+  }
   const Lens L = make_lens(2, cv.s, cv.q, 0.0, 0.0, 0.0);
   const double tau = (times[i] - cv.t0) / cv.tE;
   double sa, ca;
@@ -322,14 +363,15 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
   const double dt0 = -(d[3] * sa + d[4] * ca) / cv.tE;
   const double dtE = -tau * (d[3] * sa + d[4] * ca) / cv.tE;
   const double ct = cot ? cot[i] : 1.0;
-  double *gp = cgrad + c * 8;
-  atomicAdd(gp + 0, ct * ds);
-  atomicAdd(gp + 1, ct * dqq);
-  atomicAdd(gp + 2, ct * d[2]);
-  atomicAdd(gp + 4, ct * du0);
-  atomicAdd(gp + 5, ct * dal);
-  atomicAdd(gp + 6, ct * dt0);
-  atomicAdd(gp + 7, ct * dtE);
+  double *gp = grow + i * 8;
+  gp[0] = ct * ds;
+  gp[1] = ct * dqq;
+  gp[2] = ct * d[2];
+  gp[3] = 0.0;  // the hexadecapole of mag() takes no limb darkening (lightcurve.py:215)
+  gp[4] = ct * du0;
+  gp[5] = ct * dal;
+  gp[6] = ct * dt0;
+  gp[7] = ct * dtE;
 }
 
 template <int PREC>
@@ -340,7 +382,7 @@ cudaError_t launch_lc_points_batched_p(const EsParams &P, int64_t n, double *mag
   if (grad)
     lc_points_batched_kernel<PREC, true><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n,
                                                                           mag, route, status, P.itmax, qcount, qlist,
-                                                                          P.cot, P.cgrad);
+                                                                          P.cot, P.grow);
   else
     lc_points_batched_kernel<PREC, false><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n,
                                                                            mag, route, status, P.itmax, qcount, qlist,

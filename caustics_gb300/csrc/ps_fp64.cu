@@ -7,7 +7,7 @@ template cudaError_t launch_ea_solve_p<FP64>(const double *, const double *, dou
 template cudaError_t launch_mag_ps_p<FP64>(const Lens &, const double *, double *, double *, uint32_t *, int64_t, int,
                                            uint32_t *, cudaStream_t);
 template cudaError_t launch_lc_points_p<FP64>(const Lens &, double, const double *, double, double *, uint8_t *,
-                                              int64_t, int, uint32_t *, cudaStream_t);
+                                              int64_t, int, uint32_t *, int, cudaStream_t);
 template cudaError_t launch_lc_points_batched_p<FP64>(const EsParams &, int64_t, double *, uint8_t *, uint32_t *,
                                                       unsigned long long *, int64_t *, bool, cudaStream_t);
 }  // namespace cgb

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define CGB_ABI_VERSION 2
+#define CGB_ABI_VERSION 3
 
 /* launch status */
 #define CGB_OK 0
@@ -38,7 +38,12 @@ extern "C" {
 #define CGB_ST_AMBIGUOUS 2u  /* a lens-equation residual within x30 of the 1e-6 image threshold */
 #define CGB_ST_FALLBACK 4u   /* the mixed solver fell back to FP64 Aberth */
 #define CGB_ST_MERGE 8u      /* contour linking left open segments / overflowed */
-#define CGB_ST_CAPACITY 16u  /* limb or contour buffers too small */
+#define CGB_ST_CAPACITY 16u  /* limb or contour buffers too small (cannot arise at the accepted npts_limb:
+                                the contour buffer holds every limb image plus the closing points) */
+#define CGB_ST_INVALID 32u   /* non-finite input (source position, coefficient, time, curve parameter) or, in the
+                                batched entry points, a curve with s, q or rho not positive or tE zero: the item
+                                is not evaluated and its outputs are NaN (the reference returns NaN or garbage
+                                for such inputs) */
 
 /* Lens parameters exactly as the reference's keyword arguments:
  * binary (nlenses=2): s, q;  triple (nlenses=3): s, q, q3, r3, psi
@@ -69,6 +74,13 @@ typedef struct cgb_es_options {
   double grad_fp64_above; /* mixed-precision adjoints: a contour point whose image tangents |dz/dtheta|
                              (own or neighbours', ~1/|det J|) exceed this runs its limb-darkening
                              quadrature in FP64; 0 = default (2), < 0 = every point in FP64 */
+  int32_t triple_routing; /* cgb_mag with triple lenses: 0 = contour integral at every point, as the
+                             reference's mag() (src/caustics/lightcurve.py:226-227); 1 = the reference's
+                             triple hexadecapole (src/caustics/multipole.py:220-229) and the triple branch of its
+                             proximity test as written (lightcurve.py:37-46: third-lens terms at -r3, f''
+                             term e3/(z+r3)^3), which accepts points where the hexadecapole is tens of percent
+                             off; 2 = the same test with the third lens where the lens equation puts it (r3)
+                             and f'' = -2 sum eps_j/(z - r_j)^3 */
 } cgb_es_options;
 
 /* Parameters of one binary-lens light curve for the batched entry points: lens
@@ -99,6 +111,14 @@ int cgb_gauss_legendre(int32_t n, double *x, double *w);
  * ehrlich_aberth primitive (src/caustics/ehrlich_aberth_primitive.py:98-244). */
 int cgb_ea_solve(const double *coeffs, const double *roots_init, double *roots, int64_t n, int32_t deg,
                  int32_t itmax, int32_t precision, uint32_t *status, void *stream);
+
+/* Coefficients of the lens-equation polynomial of n source positions w
+ * (complex128[n], the centre-of-mass frame of the other entry points; shifted
+ * by x_cm = s(1-q)/(2(1+q)) as mag_point_source does): coeffs complex128[n,
+ * nlenses^2 + 2], low -> high (the order cgb_ea_solve takes), FP64.  Replaces
+ * _poly_coeffs_binary / _poly_coeffs_triple (src/caustics/point_source.py:17-86,
+ * 89-1479, highest order first there), computed in product form. */
+int cgb_lens_polynomial(const double *w, double *coeffs, int64_t n, cgb_lens_params lens, void *stream);
 
 /* Implicit-function derivatives of the roots returned by cgb_ea_solve, the
  * JVP rule of the reference's primitive (src/caustics/ehrlich_aberth_primitive.py:252-312):
@@ -211,18 +231,32 @@ int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_
  * device), so npoints is limited to 262,144 (larger calls fail with
  * CGB_ERR_UNSUPPORTED).  The first call on a device resolves the array's
  * address in that device's context (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls on one device share the array: two
+ * before any stream capture.  The address is kept per device ordinal for the
+ * life of the process: it does not survive a cudaDeviceReset or a primary
+ * context reset, after which this entry point must not be called again.
+ * `stream` must belong to the current device (a stream of another device is
+ * refused with CGB_ERR_INVALID).  All calls on one device share the array: two
  * calls in flight at the same time (other streams or threads) race on it and
  * must be serialised by the caller.  No counterpart in the reference. */
 int cgb_mag_lc_batched_noalloc(const int64_t *offsets, const double *t, const cgb_curve_params *curves,
                                int64_t ncurves, int64_t npoints, double *mag, uint8_t *route, uint32_t *status,
                                const cgb_es_options *opts, void *stream);
 
+/* Workspace (device bytes) of cgb_mag_lc_batched_vjp for npoints points: that
+ * of cgb_mag_lc_batched (16 + 16 npoints) plus one 64-byte gradient row per
+ * point (16 + 80 npoints). */
+size_t cgb_mag_lc_batched_vjp_workspace_bytes(int64_t npoints);
+
 /* Vector-Jacobian product of cgb_mag_lc_batched: grad float64[ncurves, 8] =
  * sum over the curve's points of cot[i] * d mag_i / d(s, q, rho, u1, u0,
  * alpha, t0, tE).  Hand-written adjoint: implicit-function rule for the images,
  * forward-mode tangents through the hexadecapole, reverse mode through the
- * contour integral with the contours recomputed.  Also writes mag and route. */
+ * contour integral with the contours recomputed.  Also writes mag and route.
+ * Every sum runs in a fixed order, so repeated calls give identical bits.
+ * workspace: cgb_mag_lc_batched_vjp_workspace_bytes(npoints) device bytes.
+ * The reference gets this gradient from JAX autodiff of mag()
+ * (src/caustics/lightcurve.py:99-254) through its primitive's JVP
+ * (src/caustics/ehrlich_aberth_primitive.py:254-324). */
 int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
                            int64_t npoints, const double *cot, double *grad, double *mag, uint8_t *route,
                            uint32_t *status, const cgb_es_options *opts, void *workspace, size_t workspace_bytes,

@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 def test_host_entry_points(lib):
     from caustics_gb300 import _lib as L
-    assert lib.cgb_abi_version() == 2
+    assert lib.cgb_abi_version() == 3
     for n in (2, 7, 50, 100):
         x = np.zeros(n)
         w = np.zeros(n)
@@ -51,6 +51,7 @@ def test_host_entry_points(lib):
         xr, wr = np.polynomial.legendre.leggauss(n)
         assert np.allclose(np.sort(x), xr, atol=1e-14) and np.allclose(w[np.argsort(x)], wr, atol=1e-14)
     assert lib.cgb_mag_lc_batched_workspace_bytes(1000) >= 16 + 8 * 1000
+    assert lib.cgb_mag_lc_batched_vjp_workspace_bytes(1000) == 16 + 80 * 1000
     assert L.CGB_ERR_UNSUPPORTED == 3
 
 
