@@ -487,9 +487,22 @@ def main():
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="default launch shape, no autotuner")
     ap.add_argument("--quick", action="store_true", help="headline steps only: no e2e, VJP, CPU baseline or extras")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-vjp", action="store_true",
+                    help="one VJP call on --vjp-curves curves of the gradient workload (profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.only_vjp:
+        import torch
+        import caustics_gb300 as C
+        off, t, cv = draw_batched(256, 3, 1000, 1000, args.vjp_curves)
+        cot = np.random.default_rng(3).normal(size=len(t))
+        t0 = time.perf_counter()
+        g, _ = C.mag_lc_batched_vjp(off, t, cv, cot, precision="mixed", **LC)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_vjp": True, "points": len(t), "s": time.perf_counter() - t0,
+                          "grad_finite": bool(torch.isfinite(g).all())}))
         return
     if args.quick:
         args.no_cpu = True
