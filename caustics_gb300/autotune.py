@@ -1,17 +1,24 @@
 """Launch-shape autotuner for the batched light-curve kernels.
 
 Tunes, by timing candidates on (a sample of) the caller's workload:
-* the persistent grid of the contour kernel (CTAs per SM),
-* the device work-queue chunk (items taken per queue grab),
+* threads per contour-kernel CTA (128 or 256): with one CTA per extended-source
+  evaluation this sets how many limb points and contour points a block works
+  on at once, and how many evaluations share an SM;
+* the persistent grid of the contour kernel (occupancy-sized, or one CTA per SM);
+* the device work-queue chunk (items taken per queue grab);
 * the lanes that share one contour point's Gauss-Legendre nodes.
-Results are cached per (device, npts_limb, limb darkening, npts_ld, precision).
+Results are cached per (device, npts_limb, limb darkening, npts_ld, precision,
+labelling, workload size bucket, share of points on curves with q < 0.01): the
+last two decide how many evaluations reach the contour kernel and how uneven
+they are.
 """
 import itertools
+import math
 
 import numpy as np
 import torch
 
-DEFAULT = dict(grid=0, queue_chunk=1, ld_group=1)
+DEFAULT = dict(grid=0, queue_chunk=1, ld_group=1, cta_threads=0)
 _CACHE = {}
 
 
@@ -23,6 +30,18 @@ def _sample(offsets, t, curves, max_points):
     return offsets[:c + 1], t[:n], curves[:c]
 
 
+def cache_key(dev, offsets, curves, **kw):
+    """(device, options..., log2 bucket of the point count, share of points on
+    curves with q < 0.01 in tenths)."""
+    off = offsets.cpu().numpy()
+    lens = np.diff(off)
+    q = curves[:, 1].cpu().numpy()
+    n = int(off[-1])
+    small_q = float((lens * (q < 0.01)).sum()) / max(n, 1)
+    return (torch.cuda.get_device_name(dev), tuple(sorted(kw.items())), int(math.log2(max(n, 1))),
+            int(round(10 * small_q)))
+
+
 def tune(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500, precision="mixed",
          max_points=4096, reps=2, verbose=False, labelling="reference"):
     from . import api
@@ -30,17 +49,19 @@ def tune(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, r
     t, _ = api._to_device(t, torch.float64)
     curves, _ = api._to_device(curves, torch.float64)
     dev = t.device
-    key = (torch.cuda.get_device_name(dev), int(npts_limb), bool(limb_darkening), int(npts_ld), str(precision),
-           str(labelling))
+    kw = dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=roots_itmax,
+              precision=precision, labelling=labelling)
+    key = cache_key(dev, offsets, curves, **kw)
     if key in _CACHE:
         return dict(_CACHE[key])
     so, st, sc = _sample(offsets, t, curves, max_points)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    kw = dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=roots_itmax,
-              precision=precision, labelling=labelling)
+    cands = []
+    for threads, chunk, group in itertools.product((128, 256), (1, 2, 4), (1, 2, 4)):
+        cands.append(dict(grid=0, queue_chunk=chunk, ld_group=group, cta_threads=threads))
+    cands += [dict(grid=sms, queue_chunk=c, ld_group=g, cta_threads=256) for c, g in itertools.product((1, 2), (1, 2))]
     best, best_ms, table = None, float("inf"), []
-    for per_sm, chunk, group in itertools.product((1, 2), (1, 2, 4), (1, 2, 4)):
-        cfg = dict(grid=per_sm * sms, queue_chunk=chunk, ld_group=group)
+    for cfg in cands:
         api.mag_lc_batched(so, st, sc, **kw, **cfg)
         ms = []
         for _ in range(reps):

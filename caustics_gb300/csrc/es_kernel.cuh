@@ -36,8 +36,13 @@
 
 namespace cgb {
 
-constexpr int ES_THREADS = 256;
-constexpr int ES_WARPS = ES_THREADS / 32;
+// Threads of a contour-kernel CTA: chosen at launch (128 or 256; 128 lets four
+// CTAs share an SM where their shared memory allows, for more independent
+// evaluations in the latency-bound phases); device code reads blockDim.x.
+constexpr int ES_MAX_THREADS = 256;
+constexpr int ES_MAX_WARPS = ES_MAX_THREADS / 32;
+#define ES_THREADS ((int)blockDim.x)
+#define ES_WARPS ((int)blockDim.x >> 5)
 constexpr int MAX_SEG = 30;      // 3 * n_images for triple lenses
 constexpr int MAX_PIECES = 24;   // 1 + up to 20 merges per contour
 constexpr int N_CONTOURS = 3;    // merged contours (extended_source.py:871)
@@ -1258,14 +1263,14 @@ __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsPara
 }
 
 template <int NL, int PREC, bool GRAD = false>
-__global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
+__global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                         const int64_t *__restrict__ index,
                                                         const uint8_t *__restrict__ route, int64_t npoints,
                                                         double *__restrict__ mag, uint32_t *__restrict__ status) {
   constexpr int DEG = NL * NL + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int warp_tot[ES_WARPS];
-  __shared__ double contour_acc[ES_WARPS][MAX_CLOSED + N_CONTOURS];
+  __shared__ int warp_tot[ES_MAX_WARPS];
+  __shared__ double contour_acc[ES_MAX_WARPS][MAX_CLOSED + N_CONTOURS];
   __shared__ cd centroid[MAX_CLOSED + N_CONTOURS];
   __shared__ int cstart[MAX_CLOSED + N_CONTOURS + 1];
   __shared__ int cpar[MAX_CLOSED + N_CONTOURS];
@@ -1276,15 +1281,15 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
                              // iterations; refinement FP32-stage iterations, refinement points
   __shared__ long long dbg_b[ES_DBG_SUB];  // diagnostics: refinement clocks (gaps+rank+scan, FP32 stages or
                                            // whole solves, polish + filter, per-point labelling, faithful, insertion)
-  __shared__ long long dbg_arr[ES_WARPS];  // diagnostics: each warp's clock on reaching a barrier
+  __shared__ long long dbg_arr[ES_MAX_WARPS];  // diagnostics: each warp's clock on reaching a barrier
   __shared__ long long clk[8];
   __shared__ int64_t item_sh, iord_sh;  // point index, item ordinal
   __shared__ EsItem item;
   __shared__ double cgr[MAX_CLOSED + N_CONTOURS][2];  // adjoint: dT/dx0_c, dT/dy0_c
   // adjoint partial sums per warp (summed in warp order): dT/d(x0_c, y0_c) and
   // the direct dT/d(rho, u1, w0x, w0y, a, e1)
-  __shared__ double cgr_w[GRAD ? ES_WARPS : 1][MAX_CLOSED + N_CONTOURS][2];
-  __shared__ double pgr_w[GRAD ? ES_WARPS : 1][6];
+  __shared__ double cgr_w[GRAD ? ES_MAX_WARPS : 1][MAX_CLOSED + N_CONTOURS][2];
+  __shared__ double pgr_w[GRAD ? ES_MAX_WARPS : 1][6];
   __shared__ double tot_sh;
   __shared__ float glf[2][2][GL_MAX];  // FP32 Gauss-Legendre tables [half][nodes | weights][j]
   for (int i = threadIdx.x; i < 2 * GL_MAX; i += ES_THREADS) {
@@ -2180,7 +2185,7 @@ __global__ void __launch_bounds__(ES_THREADS, NL == 2 ? 2 : 1) es_kernel(const E
       }
       cgr[c][0] = cgr[c][1] = 0.0;
     }
-    if (GRAD && tid < 6 * ES_WARPS) pgr_w[tid / 6][tid % 6] = 0.0;
+    if (GRAD && tid < 6 * ES_MAX_WARPS) pgr_w[tid / 6][tid % 6] = 0.0;
     if (P.ld) {
       // centroids (sum over all points incl. the closing point) / count
       for (int c = warp; c < ncont; c += ES_WARPS) {
@@ -2291,13 +2296,14 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
                               double *mag, uint32_t *status, int grid, cudaStream_t stream) {
   size_t smem = es_smem_bytes(P, NL, GRAD);
   auto k = es_kernel<NL, PREC, GRAD>;
+  const int threads = P.threads > 0 ? P.threads : ES_MAX_THREADS;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (grid <= 0) {  // persistent: as many CTAs as fit on the device
     int dev = 0, sms = 1, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, ES_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
     grid = sms * (per_sm > 0 ? per_sm : 1);
   }
   if (P.perm0 && !P.nearest) {
@@ -2312,7 +2318,7 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
     // ordering kernel runs and waits for it only where it reads perm0
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(ES_THREADS);
+    cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
@@ -2322,7 +2328,7 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k, P, w0, index, route, n, mag, status);
   }
-  k<<<grid, ES_THREADS, smem, stream>>>(P, w0, index, route, n, mag, status);
+  k<<<grid, threads, smem, stream>>>(P, w0, index, route, n, mag, status);
   return cudaGetLastError();
 }
 
