@@ -146,7 +146,7 @@ def test_autotuned_graph_evaluator():
     off, t, cv = draw_curves(6, seed=11)
     ev = C.BatchedLightCurves(off, t, curves_for_tuning=cv, precision="mixed", **OPTS)
     assert ev.graph is not None, ev.graph_error
-    assert set(ev.config) == {"grid", "queue_chunk", "ld_group"}
+    assert set(ev.config) == {"grid", "queue_chunk", "ld_group", "cta_threads"}
     for seed in (11, 12):
         _, _, cv2 = draw_curves(6, seed=seed)
         m = ev(torch.as_tensor(cv2, device="cuda")).cpu().numpy()
@@ -157,7 +157,8 @@ def test_autotuned_graph_evaluator():
 
 
 @pytest.mark.parametrize("cfg", [dict(grid=7, queue_chunk=3, ld_group=4), dict(grid=1, queue_chunk=1, ld_group=8),
-                                 dict(grid=0, queue_chunk=2, ld_group=2)])
+                                 dict(grid=0, queue_chunk=2, ld_group=2), dict(grid=0, cta_threads=128),
+                                 dict(grid=5, cta_threads=64, ld_group=2)])
 def test_launch_shapes_agree(cfg):
     """Every launch shape the autotuner can pick gives the same magnifications."""
     off, t, cv = draw_curves(5, seed=13)
