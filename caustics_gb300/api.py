@@ -463,17 +463,16 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
                              roots_itmax=2500, precision=None, grid=0, grad_fp64_above=0.0, labelling="reference",
                              **params):
     """(mag [n], grad [n, 6]) with grad = d mag / d(s, q, rho, u1, Re w0, Im w0)
-    (binary lenses): the hand-written adjoint of mag_extended_source.
+    for binary lenses, grad [n, 9] with d mag / d(q3, r3, psi) appended for
+    triple lenses: the hand-written adjoint of mag_extended_source.
     grad_fp64_above: in "mixed", contour points whose image tangents exceed it
     run the adjoint quadrature in FP64 (0 = default, < 0 = all)."""
-    if nlenses != 2:
-        raise ValueError("the adjoint supports binary lenses")
     wt, was_np = _to_device(np.atleast_1d(w0) if np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor) else w0,
                             torch.complex128)
     wf = wt.reshape(-1).contiguous()
     n = wf.numel()
     mag_out = torch.empty(n, dtype=torch.float64, device=wf.device)
-    g = torch.empty((n, 6), dtype=torch.float64, device=wf.device)
+    g = torch.empty((n, 6 if nlenses == 2 else 9), dtype=torch.float64, device=wf.device)
     opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid,
                        grad_fp64_above=grad_fp64_above, labelling=labelling)
     with torch.cuda.device(wf.device):

@@ -311,13 +311,22 @@ int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho
 int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, int64_t n, double rho,
                                  cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status, void *stream) {
   if (n < 0 || (n > 0 && (!w0 || !mag || !grad))) return fail(CGB_ERR_INVALID, "invalid buffers%s");
-  if (lens.nlenses != 2) return fail(CGB_ERR_UNSUPPORTED, "the adjoint supports binary lenses%s");
   EsParams P;
   int rc = make_es_params(lens, rho, opts, P);
   if (rc) return rc;
+  if (lens.nlenses == 3) {  // the adjoint's accumulators may need shared memory beyond the forward's
+    int dev = 0, maxsmem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (maxsmem > 0 && es_smem_bytes(P, 3, true) + 4096 > (size_t)maxsmem)
+      return fail(CGB_ERR_UNSUPPORTED, "npts_limb too large for the triple-lens adjoint's shared memory%s");
+  }
   P.gout = grad;
   P.s_user = lens.s;
   P.q_user = lens.q;
+  P.q3_user = lens.q3;
+  P.r3_user = lens.r3;
+  P.psi_user = lens.psi;
   int grid = opts->grid > 0 ? opts->grid : (int)((n < 4 * sm_count()) ? n : 4 * sm_count());
   if (grid < 1) grid = 1;
   return cuda_status(launch_es_grad(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),

@@ -56,13 +56,15 @@ struct EsParams {
   // kernel orders it itself
   const uint64_t *perm0;
   // adjoint (GRAD kernels): per-point gradient rows [n][6] of
-  // (s, q, rho, u1, Re w, Im w), or for batched light curves the cotangent
+  // (s, q, rho, u1, Re w, Im w) ([n][9] with (q3, r3, psi) for triple lenses),
+  // or for batched light curves the cotangent
   // weighted sum per curve [ncurves][8] of (s, q, rho, u1, u0, alpha, t0, tE)
   double *gout;
   const double *cot;
   double *grow;   // batched adjoint: cotangent-weighted gradient row [npoints][8] per point
   double *cgrad;
   double s_user, q_user;  // single-lens parameters (for the adjoint's chain rule)
+  double q3_user, r3_user, psi_user;  // triple lenses: the third lens (adjoint chain rule)
   double *dbg;  // optional per-point diagnostics (cgb_debug_extended_source), stride ES_DBG_STRIDE(Lcap)
   double gl_x[2][GL_MAX], gl_w[2][GL_MAX];
 };

@@ -822,14 +822,43 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst 
 // parameters (rho, u1, Re w0, Im w0, a, e1), differentiating through the node
 // positions, the split point and the brightness profile exactly as the
 // discretised integral depends on them.
+// Parameter directions of the adjoint: rho, u1, Re w0, Im w0, then the lens:
+// binary (a, e1): lenses at +-a with masses e1, 1 - e1; triple (a, e1, e2,
+// Re r3, Im r3): masses e1, e2, 1 - e1 - e2 at a, -a, r3.
+template <int NL>
+struct GradDirs {
+  static constexpr int NLENS = NL == 2 ? 2 : 5;
+  static constexpr int NK = 4 + NLENS;
+};
+constexpr int NK_MAX = 9;
+
+template <int NK>
 struct PQGrad {
   double P, Q;
   double Px, Py, Pa;  // dP/dx_i, dP/dy_i, dP/dy0
   double Qx, Qy, Qa;  // dQ/dx_i, dQ/dy_i, dQ/dx0
-  double Pk[6], Qk[6];  // rho, u1, Re w0, Im w0, a, e1
+  double Pk[NK], Qk[NK];  // the parameter directions (GradDirs)
 };
 
-enum { GK_RHO = 0, GK_U1 = 1, GK_WX = 2, GK_WY = 3, GK_A = 4, GK_E1 = 5 };
+enum { GK_RHO = 0, GK_U1 = 1, GK_WX = 2, GK_WY = 3, GK_A = 4, GK_E1 = 5, GK_E2 = 6, GK_R3X = 7, GK_R3Y = 8 };
+
+// d lens_eq / d theta at a fixed image position for the lens directions,
+// from u_j = 1 / (conj(z) - conj(r_j)): d/d eps_j = -u_j, d/d conj(r_j) =
+// -eps_j u_j^2 (lens_eq = z - sum_j eps_j / (conj(z) - conj(r_j))).
+template <int NL, typename R, typename C>
+__device__ __forceinline__ void lens_shifts(const C (&u)[NL], const R (&ej)[NL], C (&ds)[GradDirs<NL>::NLENS]) {
+  const C fa = u[0] * u[0] * ej[0] - u[1] * u[1] * ej[1];
+  ds[0] = C{-fa.x, -fa.y};  // a: r_0 = a, r_1 = -a
+  if constexpr (NL == 2) {
+    ds[1] = u[1] - u[0];  // e1: eps_0 = e1, eps_1 = 1 - e1
+  } else {
+    ds[1] = u[2] - u[0];  // e1: eps_0 = e1, eps_2 = 1 - e1 - e2
+    ds[2] = u[2] - u[1];  // e2: eps_1 = e2, eps_2 = 1 - e1 - e2
+    const C t = u[2] * u[2] * ej[2];
+    ds[3] = C{-t.x, -t.y};  // Re r3: conj(r3) moves by dx
+    ds[4] = C{-t.y, t.x};   // Im r3: conj(r3) moves by -i dy
+  }
+}
 
 __device__ __forceinline__ void split_point_grad(double a, double b, double rho, double &sp, double &da, double &db,
                                                  double &drho) {
@@ -853,17 +882,18 @@ __device__ __forceinline__ void split_point_grad(double a, double b, double rho,
   }
 }
 
-template <typename R, typename C>
-__device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad &g,
+template <int NL, typename R, typename C>
+__device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad<GradDirs<NL>::NK> &g,
                            const float (*glf)[2][GL_MAX]) {
-  // shifted lens equation around the contour point (binary: r_0 = a, r_1 = -a)
+  constexpr int NK = GradDirs<NL>::NK, NLD = GradDirs<NL>::NLENS;
+  // shifted lens equation around the contour point
   const double rho = It.rho, inv_rho = 1.0 / rho;
-  const cd uc64 = (lens_eq<2>(It.L, zc) - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
+  const cd uc64 = (lens_eq<NL>(It.L, zc) - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
   C uc = C{(R)uc64.x, (R)uc64.y};
-  C Dj[2], iDj[2];
-  R ej[2];
+  C Dj[NL], iDj[NL];
+  R ej[NL];
 #pragma unroll
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < NL; ++k) {
     cd d = conj(zc) - conj(It.L.r[k]);
     cd id = crecip(d);
     Dj[k] = C{(R)d.x, (R)d.y};
@@ -881,14 +911,18 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
     const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
     double sp, dsa, dsb, dsr;
     split_point_grad(a, b, rho, sp, dsa, dsb, dsr);
-    double val = 0.0, fixed = 0.0, kk[6] = {0, 0, 0, 0, 0, 0}, dlo[2], dhi[2];
+    double val = 0.0, fixed = 0.0, kk[NK], dlo[2], dhi[2];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) kk[k] = 0.0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const double lo = half ? sp : a, hi = half ? b : sp;
       const R lo_r = (R)(lo - b), hi_r = (R)(hi - b);
       const R hw = (R)0.5 * (hi_r - lo_r), mid = (R)0.5 * (hi_r + lo_r);
       const int n = half ? P.n2 : P.n1;
-      R A = 0, Bl = 0, Bh = 0, Cf = 0, Ck[6] = {0, 0, 0, 0, 0, 0};
+      R A = 0, Bl = 0, Bh = 0, Cf = 0, Ck[NK];
+#pragma unroll
+      for (int k = 0; k < NK; ++k) Ck[k] = 0;
       for (int j = 0; j < n; ++j) {
         R t, w;
         if constexpr (sizeof(R) == sizeof(float)) {
@@ -902,9 +936,9 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         const C cdl = isQ ? C{d, (R)0} : C{(R)0, -d};  // conj(delta)
         // s/rho = uc + delta/rho + sum eps conj(delta) / (D (D + conj(delta))) / rho
         C dl = isQ ? C{d * irho, (R)0} : C{(R)0, d * irho};
-        C u[2];
+        C u[NL];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < NL; ++k) {
           u[k] = crecip(Dj[k] + cdl);
           dl = dl + cdl * u[k] * iDj[k] * (ej[k] * irho);
         }
@@ -928,9 +962,11 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         // unit vector of s, and d r = Re(conj(shat) ds) / rho
         const R ir = r > (R)0 ? (R)1 / r : (R)0;
         const C sh = C{srho.x * ir, srho.y * ir};
-        const C lam = u[0] * u[0] * ej[0] + u[1] * u[1] * ej[1];
-        const C fa = u[0] * u[0] * ej[0] - u[1] * u[1] * ej[1];
-        const C fe = u[0] - u[1];
+        C lam = u[0] * u[0] * ej[0];
+#pragma unroll
+        for (int k = 1; k < NL; ++k) lam = lam + u[k] * u[k] * ej[k];
+        C dsl[NLD];
+        lens_shifts<NL, R, C>(u, ej, dsl);
         // d s / d x' = 1 + lam ; d s / d y' = i (1 - lam)
         const R drx = (sh.x * ((R)1 + lam.x) + sh.y * lam.y) * irho;
         const R dry = (sh.x * lam.y + sh.y * ((R)1 - lam.x)) * irho;
@@ -945,13 +981,13 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         Ck[GK_U1] += w * dIdu1;
         Ck[GK_WX] += w * dIdr * (-sh.x * irho);
         Ck[GK_WY] += w * dIdr * (-sh.y * irho);
-        Ck[GK_A] += w * dIdr * (-(sh.x * fa.x + sh.y * fa.y) * irho);
-        Ck[GK_E1] += w * dIdr * (-(sh.x * fe.x + sh.y * fe.y) * irho);
+#pragma unroll
+        for (int m = 0; m < NLD; ++m) Ck[GK_A + m] += w * dIdr * ((sh.x * dsl[m].x + sh.y * dsl[m].y) * irho);
       }
       val += (double)hw * (double)A;
       fixed += (double)hw * (double)Cf;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) kk[k] += (double)hw * (double)Ck[k];
+      for (int k = 0; k < NK; ++k) kk[k] += (double)hw * (double)Ck[k];
       dlo[half] = -0.5 * (double)A + (double)hw * (double)Bl;
       dhi[half] = 0.5 * (double)A + (double)hw * (double)Bh;
     }
@@ -965,33 +1001,47 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
       g.Pa = f * d_a;
       g.Px = f * fixed;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) g.Pk[k] = f * kk[k];
+      for (int k = 0; k < NK; ++k) g.Pk[k] = f * kk[k];
     } else {
       g.Q = f * val;
       g.Qx = f * d_b;
       g.Qa = f * d_a;
       g.Qy = f * fixed;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) g.Qk[k] = f * kk[k];
+      for (int k = 0; k < NK; ++k) g.Qk[k] = f * kk[k];
     }
   }
 }
 
 
-// Tangents dz/dtheta of a binary-lens image z on the limb point of angle th,
-// for theta = (rho, u1, Re w0, Im w0, a, e1): from lens_eq(z) = w0 + rho e^{i th},
-// dz = (g - lam conj(g)) / (1 - |lam|^2), lam = sum_j eps_j / (conj(z) - r_j)^2,
-// g = the source-plane shift the parameter produces at fixed z.
-__device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th, cd t[6]) {
-  const cd u0 = crecip(conj(z) - I.L.r[0]), u1 = crecip(conj(z) - I.L.r[1]);
-  const cd lam = u0 * u0 * I.L.eps[0] + u1 * u1 * I.L.eps[1];
+// Tangents dz/dtheta of an image z on the limb point of angle th, for the
+// parameter directions of GradDirs: from lens_eq(z) = w0 + rho e^{i th},
+// dz = (g - lam conj(g)) / (1 - |lam|^2), lam = sum_j eps_j / (conj(z) - conj(r_j))^2,
+// g = the source-plane shift the parameter produces at fixed z (w0 and rho
+// move the source; the lens directions move the lens equation by -lens_shifts).
+template <int NL>
+__device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th, cd (&t)[GradDirs<NL>::NK]) {
+  constexpr int NLD = GradDirs<NL>::NLENS;
+  cd u[NL];
+  double ej[NL];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    u[k] = crecip(conj(z) - conj(I.L.r[k]));
+    ej[k] = I.L.eps[k];
+  }
+  cd lam = u[0] * u[0] * ej[0];
+#pragma unroll
+  for (int k = 1; k < NL; ++k) lam = lam + u[k] * u[k] * ej[k];
   const double iD = 1.0 / (1.0 - norm2(lam));
   double sn, cs;
   sincos(th, &sn, &cs);
-  const cd g[6] = {mk(cs, sn), mk(0.0, 0.0), mk(1.0, 0.0), mk(0.0, 1.0),
-                   u0 * u0 * I.L.eps[0] - u1 * u1 * I.L.eps[1], u0 - u1};
+  cd dsl[NLD];
+  lens_shifts<NL, double, cd>(u, ej, dsl);
+  cd g[4 + NLD] = {mk(cs, sn), mk(0.0, 0.0), mk(1.0, 0.0), mk(0.0, 1.0)};
 #pragma unroll
-  for (int k = 0; k < 6; ++k) t[k] = (g[k] - lam * conj(g[k])) * iD;
+  for (int m = 0; m < NLD; ++m) g[4 + m] = mk(-dsl[m].x, -dsl[m].y);
+#pragma unroll
+  for (int k = 0; k < 4 + NLD; ++k) t[k] = (g[k] - lam * conj(g[k])) * iD;
 }
 
 // Backward pass of one extended-source evaluation (binary lenses): the
@@ -1001,9 +1051,9 @@ template <int NL, int PREC>
 __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsItem &I, int ncont, int ntot,
                             const int *cstart, const int *cpar, const cd *centroid,
                             double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2],
-                            double (*cgr_w)[MAX_CLOSED + N_CONTOURS][2], double (*pgr_w)[6], double *tot_sh,
+                            double (*cgr_w)[MAX_CLOSED + N_CONTOURS][2], double (*pgr_w)[NK_MAX], double *tot_sh,
                             int64_t pi, double *mag, const float (*glf)[2][GL_MAX]) {
-  constexpr int DEG = NL * NL + 1;
+  constexpr int DEG = NL * NL + 1, NK = GradDirs<NL>::NK;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     double tot = 0.0;
@@ -1019,7 +1069,9 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
   // pass 2: node-level derivatives, trapezoid weights, centroids, direct terms.
   // Sums over points run in a fixed order (per-thread partials, shuffle trees,
   // per-warp slots summed in warp order): two identical calls give identical bits.
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  double acc[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) acc[k] = 0.0;
   {
     int c = 0;
     for (int base = warp * 32; base < ntot; base += ES_THREADS) {  // warp-uniform trip count
@@ -1041,33 +1093,33 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
           // scattered into the neighbours' position adjoints, where it would become
           // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
           // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
-          cd tn[6], tp[6], ti[6];
+          cd tn[NK], tp[NK], ti[NK];
           const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
-          image_tangents(I, zn, S.TH[cpn / DEG], tn);
-          image_tangents(I, zp, S.TH[cpp / DEG], tp);
-          image_tangents(I, zc, S.TH[S.CP[i] / DEG], ti);
+          image_tangents<NL>(I, zn, S.TH[cpn / DEG], tn);
+          image_tangents<NL>(I, zp, S.TH[cpp / DEG], tp);
+          image_tangents<NL>(I, zc, S.TH[S.CP[i] / DEG], ti);
           // Near a critical curve the tangents grow like 1/|det J| and the
           // pointwise contributions cancel in the sum; there the FP32 node values
           // (relative error ~1e-7) would be amplified, so such points run the
           // quadrature in FP64.
           double amp2 = 0.0;
   #pragma unroll
-          for (int k = 0; k < 6; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
-          PQGrad g;
+          for (int k = 0; k < NK; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
+          PQGrad<NK> g;
           if (PREC == MIXED && amp2 <= P.grad_amp2)
-            ld_pq_grad<float, cf>(P, I, zc, centroid[c], g, glf);
+            ld_pq_grad<NL, float, cf>(P, I, zc, centroid[c], g, glf);
           else
-            ld_pq_grad<double, cd>(P, I, zc, centroid[c], g, glf);
+            ld_pq_grad<NL, double, cd>(P, I, zc, centroid[c], g, glf);
           const cd pq = mk(g.P, g.Q);
           atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
           atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
   #pragma unroll
-          for (int k = 0; k < 6; ++k)
+          for (int k = 0; k < NK; ++k)
             acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
           cg1 = pc * wx * g.Pa;
           cg0 = pc * wy * g.Qa;
   #pragma unroll
-          for (int k = 0; k < 6; ++k) acc[k] += pc * (wx * g.Pk[k] + wy * g.Qk[k]);
+          for (int k = 0; k < NK; ++k) acc[k] += pc * (wx * g.Pk[k] + wy * g.Qk[k]);
         } else if (i + 1 < e) {
           // pair (i, i+1): 1/4 [(x_i + x_{i+1})(y_{i+1} - y_i) - (y_i + y_{i+1})(x_{i+1} - x_i)];
           // each GG entry receives exactly two addends onto zero, an order-free sum
@@ -1085,7 +1137,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     }
   }
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
+  for (int k = 0; k < NK; ++k) {
     double v = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1100,7 +1152,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
   }
   __syncthreads();
   // pass 3: every contour point's image through the lens equation:
-  // dz + lam conj(dz) = dw0 + e^{i theta} drho + f_a da + f_e1 de1, lam = sum eps/(conj z - r)^2
+  // dz + lam conj(dz) = g (image_tangents), lam = sum eps/(conj z - conj r)^2
   {
     int c = 0;
     for (int i = tid; i < ntot; i += ES_THREADS) {
@@ -1112,14 +1164,14 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
         G = G + mk(cgr[c][0] * inv_n, cgr[c][1] * inv_n);
       }
       const uint32_t cp = S.CP[i];
-      cd t[6];
-      image_tangents(I, S.Z[cp], S.TH[cp / DEG], t);
+      cd t[NK];
+      image_tangents<NL>(I, S.Z[cp], S.TH[cp / DEG], t);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) acc[k] += G.x * t[k].x + G.y * t[k].y;
+      for (int k = 0; k < NK; ++k) acc[k] += G.x * t[k].x + G.y * t[k].y;
     }
   }
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
+  for (int k = 0; k < NK; ++k) {
     double v = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1130,19 +1182,35 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     const double tot = *tot_sh, rho = I.rho;
     const double mu = fabs(tot) / (3.14159265358979323846 * rho * rho);
     const double sT = (tot > 0 ? 1.0 : (tot < 0 ? -1.0 : 0.0)) / (3.14159265358979323846 * rho * rho);
-    double d[6];
-    for (int k = 0; k < 6; ++k) {
+    double d[NK];
+    for (int k = 0; k < NK; ++k) {
       double v = 0.0;
       for (int w = 0; w < ES_WARPS; ++w) v += pgr_w[w][k];
       d[k] = sT * v;
     }
     d[GK_RHO] -= 2.0 * mu / rho;
-    // (a, e1, x_cm) -> (s, q): a = s/2, e1 = 1/(1+q), x_cm = a(1-q)/(1+q)
+    // (a, e1, x_cm) -> (s, q): a = s/2, e1 = 1/(1+q), x_cm = a(1-q)/(1+q);
+    // triple (point_source.py:1807-1817): e1 = q/(1+q+q3), e2 = q e1, r3 = R e^{i psi}
     const double q = I.q, a = 0.5 * I.s, opq = 1.0 + q;
     const double ds = 0.5 * d[GK_A] + d[GK_WX] * (1.0 - q) / (2.0 * opq);
-    const double dq = -d[GK_E1] / (opq * opq) - d[GK_WX] * 2.0 * a / (opq * opq);
+    double dq;
+    if constexpr (NL == 2) {
+      dq = -d[GK_E1] / (opq * opq) - d[GK_WX] * 2.0 * a / (opq * opq);
+    } else {
+      const double den = 1.0 + q + P.q3_user, e1 = q / den;
+      const double e1_q = (1.0 + P.q3_user) / (den * den), e1_q3 = -q / (den * den);
+      dq = d[GK_E1] * e1_q + d[GK_E2] * (e1 + q * e1_q) - d[GK_WX] * 2.0 * a / (opq * opq);
+      double sp, cp;
+      sincos(P.psi_user, &sp, &cp);
+      if (P.gout) {
+        double *gp = P.gout + pi * 9;
+        gp[6] = d[GK_E1] * e1_q3 + d[GK_E2] * q * e1_q3;     // q3
+        gp[7] = d[GK_R3X] * cp + d[GK_R3Y] * sp;              // r3
+        gp[8] = P.r3_user * (-d[GK_R3X] * sp + d[GK_R3Y] * cp);  // psi
+      }
+    }
     mag[pi] = mu;
-    if (I.curve >= 0 && P.grow) {
+    if (NL == 2 && I.curve >= 0 && P.grow) {
       const CurveDev cv = P.curves[I.curve];
       const double ct = P.cot ? P.cot[pi] : 1.0;
       double sa, ca;
@@ -1165,7 +1233,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
       gp[6] = ct * dt0;
       gp[7] = ct * dtE;
     } else if (P.gout) {
-      double *gp = P.gout + pi * 6;
+      double *gp = P.gout + pi * (NL == 2 ? 6 : 9);
       gp[0] = ds;
       gp[1] = dq;
       gp[2] = d[GK_RHO];
@@ -1289,7 +1357,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
   // adjoint partial sums per warp (summed in warp order): dT/d(x0_c, y0_c) and
   // the direct dT/d(rho, u1, w0x, w0y, a, e1)
   __shared__ double cgr_w[GRAD ? ES_MAX_WARPS : 1][MAX_CLOSED + N_CONTOURS][2];
-  __shared__ double pgr_w[GRAD ? ES_MAX_WARPS : 1][6];
+  __shared__ double pgr_w[GRAD ? ES_MAX_WARPS : 1][NK_MAX];
   __shared__ double tot_sh;
   __shared__ float glf[2][2][GL_MAX];  // FP32 Gauss-Legendre tables [half][nodes | weights][j]
   for (int i = threadIdx.x; i < 2 * GL_MAX; i += ES_THREADS) {
@@ -1383,7 +1451,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
         mag[pi] = nan;
         if (status) status[pi] = route ? (status[pi] | CGB_ST_INVALID) : CGB_ST_INVALID;
         if (GRAD && P.gout)
-          for (int k = 0; k < 6; ++k) P.gout[pi * 6 + k] = nan;
+          for (int k = 0; k < (NL == 2 ? 6 : 9); ++k) P.gout[pi * (NL == 2 ? 6 : 9) + k] = nan;
       }
       __syncthreads();
       continue;
@@ -2185,7 +2253,8 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
       }
       cgr[c][0] = cgr[c][1] = 0.0;
     }
-    if (GRAD && tid < 6 * ES_MAX_WARPS) pgr_w[tid / 6][tid % 6] = 0.0;
+    if (GRAD)
+      for (int k = tid; k < NK_MAX * ES_MAX_WARPS; k += ES_THREADS) pgr_w[k / NK_MAX][k % NK_MAX] = 0.0;
     if (P.ld) {
       // centroids (sum over all points incl. the closing point) / count
       for (int c = warp; c < ncont; c += ES_WARPS) {

@@ -1,7 +1,8 @@
 // Extended-source dispatch (src/caustics/extended_source.py:741-904): picks the
 // kernel variant for the lens multiplicity and the precision.  The kernel
 // itself is in es_kernel.cuh; each variant is compiled in its own translation
-// unit (es_b64.cu, es_b32.cu, es_t64.cu, es_t32.cu).
+// unit (es_b64.cu, es_b32.cu, es_t64.cu, es_t32.cu; the adjoints es_b64g.cu,
+// es_b32g.cu, es_t64g.cu, es_t32g.cu).
 #include "es.h"
 #include "internal.h"
 #include "es_kernel.cuh"
@@ -24,6 +25,12 @@ extern template cudaError_t launch_es_variant<2, FP64, true>(const EsParams &, c
                                                              const uint8_t *, int64_t, double *, uint32_t *, int,
                                                              cudaStream_t);
 extern template cudaError_t launch_es_variant<2, MIXED, true>(const EsParams &, const cd *, const int64_t *,
+                                                              const uint8_t *, int64_t, double *, uint32_t *, int,
+                                                              cudaStream_t);
+extern template cudaError_t launch_es_variant<3, FP64, true>(const EsParams &, const cd *, const int64_t *,
+                                                             const uint8_t *, int64_t, double *, uint32_t *, int,
+                                                             cudaStream_t);
+extern template cudaError_t launch_es_variant<3, MIXED, true>(const EsParams &, const cd *, const int64_t *,
                                                               const uint8_t *, int64_t, double *, uint32_t *, int,
                                                               cudaStream_t);
 
@@ -55,8 +62,11 @@ cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t 
 cudaError_t launch_es_grad(const EsParams &P, const double *w0, const uint8_t *route, int64_t n, double *mag,
                            uint32_t *status, int precision, int grid, cudaStream_t stream) {
   if (n == 0 && !P.qhead) return cudaSuccess;
-  if (!P.curves && P.L.n != 2) return cudaErrorInvalidValue;
   const cd *w = reinterpret_cast<const cd *>(w0);
+  if (!P.curves && P.L.n == 3)
+    return precision == MIXED ? launch_es_variant<3, MIXED, true>(P, w, nullptr, route, n, mag, status, grid, stream)
+                              : launch_es_variant<3, FP64, true>(P, w, nullptr, route, n, mag, status, grid, stream);
+  if (!P.curves && P.L.n != 2) return cudaErrorInvalidValue;
   return precision == MIXED ? launch_es_variant<2, MIXED, true>(P, w, nullptr, route, n, mag, status, grid, stream)
                             : launch_es_variant<2, FP64, true>(P, w, nullptr, route, n, mag, status, grid, stream);
 }

@@ -95,7 +95,7 @@ def _(w, nlenses, s, q, q3, r3, psi, itmax, precision):
     return w.new_empty(w.shape, dtype=torch.float64)
 
 
-# ---- extended source, differentiable in (w0, s, q, rho, u1) for binary lenses ----
+# ---- extended source, differentiable in w0 and the lens, source and limb parameters ----
 
 def _es_kw(npts_limb, limb_darkening, npts_ld, itmax, precision):
     return dict(npts_limb=npts_limb, limb_darkening=limb_darkening, npts_ld=npts_ld, roots_itmax=itmax,
@@ -107,7 +107,7 @@ def mag_extended_source(w0: Tensor, params: Tensor, nlenses: int, npts_limb: int
                         npts_ld: int, itmax: int, precision: int) -> Tensor:
     """Extended-source magnification of the source centres w0 (complex128 [n]);
     params (float64): (s, q, rho, u1) for binary lenses, (s, q, rho, u1, q3, r3,
-    psi) for triple lenses."""
+    psi) for triple lenses; differentiable in w0 and params."""
     pv = [float(x) for x in params.detach().cpu()]
     lens = dict(s=pv[0], q=pv[1]) if nlenses == 2 else dict(s=pv[0], q=pv[1], q3=pv[4], r3=pv[5], psi=pv[6])
     return A.mag_extended_source(w0.contiguous(), pv[2], nlenses=nlenses, u1=pv[3],
@@ -122,24 +122,26 @@ def _(w0, params, nlenses, npts_limb, limb_darkening, npts_ld, itmax, precision)
 @torch.library.custom_op("caustics::mag_extended_source_grad", mutates_args=())
 def mag_extended_source_grad(w0: Tensor, params: Tensor, npts_limb: int, limb_darkening: bool, npts_ld: int,
                              itmax: int, precision: int) -> List[Tensor]:
-    """(mag [n], grad [n, 6]) of a binary lens, grad = d mag / d(s, q, rho, u1,
-    Re w0, Im w0); the contours are recomputed, not stored."""
-    s, q, rho, u1 = (float(x) for x in params.detach().cpu()[:4])
-    m, g = A.mag_extended_source_grad(w0.contiguous(), rho, u1=u1, s=s, q=q,
-                                      **_es_kw(npts_limb, limb_darkening, npts_ld, itmax, precision))
+    """(mag [n], grad [n, k]): binary lens (params (s, q, rho, u1)), k = 6,
+    grad = d mag / d(s, q, rho, u1, Re w0, Im w0); triple lens (params (s, q,
+    rho, u1, q3, r3, psi)), k = 9, with d mag / d(q3, r3, psi) appended.  The
+    contours are recomputed, not stored."""
+    pv = [float(x) for x in params.detach().cpu()]
+    lens = dict(s=pv[0], q=pv[1]) if len(pv) == 4 else dict(s=pv[0], q=pv[1], q3=pv[4], r3=pv[5], psi=pv[6])
+    m, g = A.mag_extended_source_grad(w0.contiguous(), pv[2], nlenses=2 if len(pv) == 4 else 3, u1=pv[3],
+                                      **_es_kw(npts_limb, limb_darkening, npts_ld, itmax, precision), **lens)
     return [m, g]
 
 
 @mag_extended_source_grad.register_fake
 def _(w0, params, npts_limb, limb_darkening, npts_ld, itmax, precision):
     n = w0.numel()
-    return [w0.new_empty((n,), dtype=torch.float64), w0.new_empty((n, 6), dtype=torch.float64)]
+    k = 6 if params.shape[0] == 4 else 9
+    return [w0.new_empty((n,), dtype=torch.float64), w0.new_empty((n, k), dtype=torch.float64)]
 
 
 def _es_setup(ctx, inputs, output):
     w0, params, nlenses, npts_limb, limb_darkening, npts_ld, itmax, precision = inputs
-    if nlenses != 2:
-        raise NotImplementedError("caustics::mag_extended_source is differentiable for binary lenses")
     ctx.save_for_backward(w0, params)
     ctx.opts = (npts_limb, limb_darkening, npts_ld, itmax, precision)
 
@@ -151,6 +153,8 @@ def _es_backward(ctx, gmag):
     gw = (gm * torch.complex(g[:, 4], g[:, 5])).reshape(w0.shape)
     gp = torch.zeros_like(params)
     gp[:4] = (gm[:, None] * g[:, :4]).sum(0)
+    if params.shape[0] == 7:  # (q3, r3, psi)
+        gp[4:] = (gm[:, None] * g[:, 6:]).sum(0)
     return gw, gp, None, None, None, None, None, None
 
 

@@ -194,8 +194,10 @@ int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t 
 int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
                             const cgb_es_options *opts, uint32_t *status, void *stream);
 
-/* Adjoint of cgb_mag_extended_source for binary lenses: mag float64[n] and
- * grad float64[n, 6] = d mag / d(s, q, rho, u1, Re w0, Im w0) of the discretised
+/* Adjoint of cgb_mag_extended_source: mag float64[n] and, for binary lenses,
+ * grad float64[n, 6] = d mag / d(s, q, rho, u1, Re w0, Im w0); for triple
+ * lenses grad float64[n, 9] = d mag / d(s, q, rho, u1, Re w0, Im w0, q3, r3, psi)
+ * (the reference's parameters, src/caustics/point_source.py:1807-1817) of the discretised
  * contour integral (the limb sampling, segment linking and merging decisions
  * are piecewise constant, as under the reference's autodiff).  The contours are
  * recomputed in the backward pass, not stored.  The reference differentiates

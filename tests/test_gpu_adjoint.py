@@ -130,3 +130,86 @@ def test_adjoint_vs_oracle_frozen_structure(G, prec):
         assert np.all(np.abs(g[0] - r2)[ok] / scale[ok] < 2e-3), (g[0], r2, ok)
         checked += ok.sum()
     assert checked >= 12
+
+
+# ---- triple lenses: d mag / d(s, q, rho, u1, Re w0, Im w0, q3, r3, psi) ----
+TRIPLE = dict(s=1.0, q=0.5, q3=0.05, r3=0.9, psi=1.1)  # the triple fixture's system (mag_es_triple)
+T_NAMES = ("s", "q", "rho", "u1", "wx", "wy", "q3", "r3", "psi")
+
+
+def _lens3(p):
+    return L.LensParams(3, p["s"], p["q"], p["q3"], p["r3"], p["psi"])
+
+
+def fwd3(w, rho, p, u1, npts, nld, ld):
+    """FP64 forward with the limb angle grid of each point (debug record)."""
+    lib = L.lib()
+    wt = torch.as_tensor(np.atleast_1d(np.asarray(w, dtype=complex))).cuda()
+    n = wt.numel()
+    mag = torch.empty(n, dtype=torch.float64, device="cuda")
+    dbg = torch.zeros((n, lib.cgb_debug_record_len(npts)), dtype=torch.float64, device="cuda")
+    rc = lib.cgb_debug_extended_source(ctypes.c_void_p(wt.data_ptr()), ctypes.c_void_p(mag.data_ptr()), n, rho,
+                                       _lens3(p), L.EsOptions(npts, int(ld), u1, nld, 2500, 0, 0), None,
+                                       ctypes.c_void_p(dbg.data_ptr()), None)
+    assert rc == 0, lib.cgb_last_error()
+    d = dbg.cpu().numpy()
+    return mag.cpu().numpy(), d[:, 63:63 + int(d[0, 0])]
+
+
+def grad3(w, rho, p, u1, npts, nld, ld, prec):
+    m, g = C.mag_extended_source_grad(np.asarray(w, dtype=complex), rho, nlenses=3, npts_limb=npts,
+                                      limb_darkening=ld, u1=u1, npts_ld=nld, precision=("fp64", "mixed")[prec], **p)
+    return m, g
+
+
+def fd3_stable(w, rho, p, u1, npts, nld, ld, k):
+    """Central differences at relative steps 1e-7 and 1e-8 (absolute for the
+    source position and psi), trusted where both agree and every evaluated limb
+    grid is the same."""
+    res = []
+    for rel in (1e-7, 1e-8):
+        name = T_NAMES[k]
+        vals = dict(p, rho=rho, u1=u1)
+        h = rel * (1.0 if name in ("wx", "wy", "psi") else max(abs(vals[name]), 1e-3))
+        out = []
+        for sgn in (1, -1):
+            pp, ww, r, uu = dict(p), np.asarray(w, dtype=complex), rho, u1
+            if name == "wx":
+                ww = ww + sgn * h
+            elif name == "wy":
+                ww = ww + 1j * sgn * h
+            elif name == "rho":
+                r = rho + sgn * h
+            elif name == "u1":
+                uu = u1 + sgn * h
+            else:
+                pp[name] = p[name] + sgn * h
+            out.append(fwd3(ww, r, pp, uu, npts, nld, ld))
+        (mp, tp), (mm, tm) = out
+        same = np.array([np.array_equal(a, b) for a, b in zip(tp, tm)])
+        res.append(((mp - mm) / (2 * h), same))
+    (f1, s1), (f2, s2) = res
+    return f2, s1 & s2 & (np.abs(f1 - f2) <= 1e-3 * np.maximum(np.abs(f2), 1e-3))
+
+
+@pytest.mark.parametrize("ld", [False, True])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_triple_adjoint_vs_central_differences(G, prec, ld):
+    d = G("mag_es_triple")
+    w, rho, npts = d["w"], float(d["rho"]), int(d["npts_limb"])
+    u1 = 0.6 if ld else 0.0
+    mag, g = grad3(w, rho, TRIPLE, u1, npts, 60, ld, prec)
+    assert g.shape == (len(w), 9)
+    if not ld:
+        assert np.max(np.abs(mag - d["mag"]) / d["mag"]) < (1e-9 if prec == 0 else 1e-4)
+        assert np.all(g[:, 3] == 0)
+    checked = 0
+    for k in range(9):
+        if k == 3 and not ld:
+            continue
+        f, ok = fd3_stable(w, rho, TRIPLE, u1, npts, 60, ld, k)
+        scale = np.maximum(np.abs(f), 1e-3 * mag)
+        err = np.abs(g[:, k] - f) / scale
+        checked += ok.sum()
+        assert np.all(err[ok] < 1e-3), (T_NAMES[k], g[ok, k], f[ok])
+    assert checked >= 8 * len(w) // 2
