@@ -734,6 +734,34 @@ def caustics_proximity_test(w, z, mask, rho, delta_mu, lens, c_m=1e-2, gamma=0.0
     return t_f & t_mc
 
 
+def caustics_proximity_test_triple(w, z, mask, rho, delta_mu, lens, as_written=True, c_m=1e-2, gamma=0.02, c_f=4.0,
+                                   rho_min=1e-3):
+    """The nlenses == 3 branch of lightcurve.py:23-75.  as_written: f, f', f''
+    exactly as the reference writes them (lightcurve.py:37-46: third-lens terms
+    at -r3 and f'' third term e3/(z+r3)^3); otherwise the third lens at r3 with
+    f'' = -2 sum eps_j/(z - r_j)^3.  w is shifted."""
+    a, e1, e2 = lens.r[0].real, lens.eps[0], lens.eps[1]
+    e3 = 1 - e1 - e2
+    r3 = -lens.r[2] if as_written else lens.r[2]
+    c3 = 1.0 if as_written else -2.0
+    f = lambda z: -e1 / (z - a) - e2 / (z + a) - e3 / (z - r3)
+    fp = lambda z: e1 / (z - a) ** 2 + e2 / (z + a) ** 2 + e3 / (z - r3) ** 2
+    fpp = lambda z: 2 * (e1 / (a - z) ** 3 - e2 / (a + z) ** 3) + c3 * e3 / (z - r3) ** 3
+    zb = np.conj(z)
+    zh = np.conj(w) - f(z)
+    fp_z, fpp_z, fp_zb, fp_zh, fpp_zb = fp(z), fpp(z), fp(zb), fp(zh), fpp(zb)
+    J = 1.0 - np.abs(fp_z * fp_zb)
+    mu_cusp = 6 * np.imag(3 * fp_zb ** 3 * fpp_z ** 2) / J ** 5 * (rho + rho_min) ** 2
+    mu_cusp = np.sum(np.abs(mu_cusp) * mask, axis=0)
+    t_mc = gamma * mu_cusp + delta_mu < c_m
+    Jh = 1 - np.abs(fp_z * fp_zh)
+    with np.errstate(all="ignore"):
+        fac = np.abs(J * Jh ** 2 / (Jh * fpp_zb * fp_z - np.conj(Jh) * fpp_z * fp_zb * fp_zh))
+    t_f = 0.5 * np.sum(~mask * fac, axis=0) > c_f * (rho + rho_min)
+    t_f = np.where(np.sum(~mask, axis=0) == 0, True, t_f)
+    return t_f & t_mc
+
+
 def planetary_caustic_test(w, rho, lens, c_p=2.0):
     """lightcurve.py:78-85, including q' = e1/(1-e1) (the inverse of q)."""
     a, e1 = lens.r[0].real, lens.eps[0]

@@ -253,3 +253,55 @@ def test_sky_projection_is_orthonormal():
     d = direction / np.linalg.norm(direction)
     assert abs(east @ north) < 1e-15 and abs(east @ d) < 1e-15 and abs(north @ d) < 1e-15
     assert abs(np.linalg.norm(east) - 1) < 1e-15 and north[2] > 0
+
+
+# ---- the fixtures at the configured workload sizes, on subsamples the oracle finishes in seconds ----
+
+@pytest.mark.parametrize("n", range(4))
+def test_triple_hexadecapole_and_proximity_pieces(G, n):
+    """The reference's triple hexadecapole (multipole.py:220-229) and the triple
+    branch of its proximity test as written (lightcurve.py:37-46)."""
+    d = G(f"hex_triple{n}")
+    L = O.Lens.triple(float(d["s"]), float(d["q"]), float(d["q3"]), float(d["r3"]), float(d["psi"]))
+    mu, dmu = O.mag_hexadecapole(d["z"], d["mask"], float(d["rho"]), L)
+    # 1e-8: the series terms W_k ~ eps_j / (z - r_j)^k of an image next to a lens
+    # of mass fraction ~1e-4 amplify the rounding of the two restatements
+    assert np.max(np.abs(mu - d["mu_multi"]) / d["mu_multi"]) < 1e-8
+    t1 = O.caustics_proximity_test_triple(d["w"] + L.x_cm, d["z"], d["mask"], float(d["rho"]), dmu, L)
+    assert np.array_equal(t1, d["test_prox"])
+
+
+def test_light_curve_2000_points_subsample(G):
+    d = G("mag_lc_binary_ld_s1.1_q5e-3_2000pt")
+    cv = d["curve"]
+    idx = np.arange(0, 2000, 200)
+    m, hex_ok = O.mag(d["w"][idx], cv[2], npts_limb=int(d["npts_limb"]), limb_darkening=True, u1=cv[3],
+                      npts_ld=int(d["npts_ld"]), s=cv[0], q=cv[1], return_route=True)
+    assert np.max(np.abs(m - d["mag"][idx]) / d["mag"][idx]) < 1e-9
+    assert np.array_equal(~hex_ok, d["route"][idx])
+
+
+def test_batched_workload_sample_subsample(G):
+    d = G("mag_lc_batched_seed2_sample")
+    off = d["offsets"]
+    for c in range(len(off) - 1):
+        idx = np.linspace(off[c], off[c + 1] - 1, 2).astype(int)
+        cv = d["curves"][c]
+        w = O.trajectory(d["t"][idx], cv[4], cv[5], cv[6], cv[7])
+        m = O.mag(w, cv[2], npts_limb=200, limb_darkening=True, u1=cv[3], npts_ld=100, s=cv[0], q=cv[1])
+        assert np.max(np.abs(m - d["mag"][idx]) / d["mag"][idx]) < 1e-9, c
+
+
+def test_triple_point_source_1000_systems_subsample(G):
+    d = G("mag_ps_triple_1000sys")
+    rng = np.random.default_rng(1)
+    s1, s2 = rng.uniform(0.5, 2.0, 1000), rng.uniform(0.5, 2.0, 1000)
+    q1, q2 = 10 ** rng.uniform(-4, 0, 1000), 10 ** rng.uniform(-4, -1, 1000)
+    psi = rng.uniform(0, 2 * np.pi, 1000)
+    x, y = rng.uniform(-1.5, 1.5, (1000, 1000)), rng.uniform(-1.5, 1.5, (1000, 1000))
+    npos = int(d["npos"])
+    for k in range(0, 1000, 25):
+        m = O.mag_point_source(x[k, :npos] + 1j * y[k, :npos], nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k],
+                               psi=psi[k], init_mode=0)
+        ok = np.isfinite(d["mag"][k]) & (d["mag"][k] > 0)
+        assert np.quantile(np.abs(m - d["mag"][k])[ok] / d["mag"][k][ok], 0.95) < 1e-9, k
