@@ -402,7 +402,19 @@ def triple_ps_1000sys_fixture(ref, procs, npos=32, nroots=2):
     nimg = np.stack([r[2].sum(axis=0) for r in res]).astype(np.uint8)
     roots = np.stack([r[1][:, :nroots].T for r in res])  # [sys, pos, 10]
     mask = np.stack([r[2][:, :nroots].T for r in res])
-    return {"mag_ps_triple_1000sys": dict(npos=np.int64(npos), mag=mag, nimg=nimg, roots=roots, mask=mask)}
+    # positions where one of the reference's own image residuals lies within x30
+    # of the 1e-6 filter threshold (point_source.py:1707): their count is decided
+    # by rounding
+    from caustics import point_source as ps
+    amb = []
+    for k, r in enumerate(res):
+        a, e1 = 0.5 * s1[k], q1[k] / (1 + q1[k] + q2[k])
+        prm = dict(a=a, r3=s2[k] * np.exp(1j * psi[k]), e1=e1, e2=q1[k] * e1)
+        wc = w[k, :npos] + a * (1 - q1[k]) / (1 + q1[k])
+        resid = np.abs(np.asarray(ps.lens_eq(r[1], nlenses=3, **prm)) - wc[None, :])
+        amb.append(np.any((resid > 1e-6 / 30) & (resid < 1e-6 * 30), axis=0))
+    return {"mag_ps_triple_1000sys": dict(npos=np.int64(npos), mag=mag, nimg=nimg, roots=roots, mask=mask,
+                                          ambiguous=np.stack(amb))}
 
 
 def hex_triple_fixture(ref, procs):

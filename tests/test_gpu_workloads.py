@@ -171,12 +171,10 @@ def test_triple_point_source_1000_systems(G):
         m, z, mask = C.mag_point_source(w[k, :npos], nlenses=3, precision="fp64", return_images=True, **p)
         lens = O.Lens.triple(p["s"], p["q"], p["q3"], p["r3"], p["psi"])
         wk = w[k, :npos] + lens.x_cm
-        amb = _ambiguous(np.moveaxis(z, -1, 0), wk, lens)
-        amb[:nroots] |= _ambiguous(d["roots"][k].T, wk[:nroots], lens)
+        amb = _ambiguous(np.moveaxis(z, -1, 0), wk, lens) | d["ambiguous"][k]
         cnt = np.array([bin(int(x)).count("1") for x in mask])
         assert np.array_equal(cnt[~amb], d["nimg"][k][~amb]), k
-        ok = ~amb & (cnt == d["nimg"][k])
-        errs.append(rel(m[ok], d["mag"][k][ok]))
+        errs.append(rel(m[~amb], d["mag"][k][~amb]))
         # roots as sets against the reference solver's
         zr = d["roots"][k]
         dist = np.min(np.abs(zr[:, :, None] - z[:nroots, None, :]), axis=-1) / np.maximum(np.abs(zr), 1.0)

@@ -301,11 +301,17 @@ def test_triple_point_source_1000_systems_subsample(G):
     x, y = rng.uniform(-1.5, 1.5, (1000, 1000)), rng.uniform(-1.5, 1.5, (1000, 1000))
     npos = int(d["npos"])
     for k in range(0, 1000, 25):
-        m = O.mag_point_source(x[k, :npos] + 1j * y[k, :npos], nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k],
-                               psi=psi[k], init_mode=0)
+        L = O.Lens.triple(s1[k], q1[k], q2[k], s2[k], psi[k])
+        w = x[k, :npos] + 1j * y[k, :npos]
+        m = O.mag_point_source(w, nlenses=3, s=s1[k], q=q1[k], q3=q2[k], r3=s2[k], psi=psi[k], init_mode=0)
+        z, mask = O.images_point_source(w + L.x_cm, L, init_mode=0)
+        res = np.abs(O.lens_eq(z, L) - (w + L.x_cm)[None, :])
+        # a residual (the oracle's or the reference's) near the 1e-6 filter
+        amb = np.any((res > 1e-6 / 30) & (res < 1e-6 * 30), axis=0) | d["ambiguous"][k]
+        assert np.array_equal(mask.sum(0)[~amb], d["nimg"][k][~amb]), k
         # the polynomial's coefficients (product form here, the 1336 expanded
         # monomials there) round differently, and images next to a lens of mass
-        # fraction ~1e-4 are conditioned like sqrt(eps): the promised 1e-4 bound
-        # everywhere, 1e-11 for most points
-        err = np.abs(m - d["mag"][k]) / d["mag"][k]
-        assert err.max() < 1e-4 and np.median(err) < 1e-11, k
+        # fraction ~1e-4 are conditioned like sqrt(eps): the promised 1e-4 bound,
+        # 1e-11 for most points
+        err = (np.abs(m - d["mag"][k]) / d["mag"][k])[~amb]
+        assert err.size == 0 or (err.max() < 1e-4 and np.median(err) < 1e-11), k
