@@ -118,7 +118,10 @@ def test_repeated_calls_are_bit_identical():
         assert torch.equal(g1, g2) and torch.equal(m1, m2)
         f1 = C.mag_lc_batched(off, t, cv, precision=prec, **LC)
         f2 = C.mag_lc_batched(off, t, cv, precision=prec, **LC)
-        assert torch.equal(f1, f2) and torch.equal(f1, m1)
+        assert torch.equal(f1, f2)
+        # the adjoint's forward runs in another kernel instantiation (its own
+        # instruction scheduling of the same arithmetic)
+        assert torch.allclose(f1, m1, rtol=1e-12, atol=0)
     w = rng.uniform(-0.2, 0.2, 16) + 1j * rng.uniform(-0.2, 0.2, 16)
     a = C.mag_extended_source_grad(w, 1e-2, s=1.1, q=5e-3, u1=0.5, precision="mixed", **LC)
     b = C.mag_extended_source_grad(w, 1e-2, s=1.1, q=5e-3, u1=0.5, precision="mixed", **LC)

@@ -86,44 +86,55 @@ def test_batched_workload_flagged_points(G, precision):
     assert m.min() < 1.0  # ... including a point the reference itself gives mu < 1
 
 
-def _trusted(J1, J2):
+def _fd_noise(mag, cv):
+    """Rounding noise of a central difference of the FP64 magnification at
+    relative step 1e-7 (mu ~1e-13 relative over 2e-7 of the parameter's scale),
+    per point and input (s, q, rho, u1, Re w, Im w), with a margin."""
+    scale = np.array([cv[0], cv[1], cv[2], cv[3], cv[2], cv[2]])
+    return 1e-5 * mag[:, None] / scale[None, :]
+
+
+def _trusted(J1, J2, noise):
     """Points whose six central-difference derivatives agree between the two
     steps (the limb refinement, a discrete choice, did not change within +-h)."""
-    scale = np.maximum(np.abs(J1), np.abs(J2))
-    return np.all(np.abs(J1 - J2) <= 2e-4 * scale + 1e-12, axis=1)
+    return np.all(np.abs(J1 - J2) <= 2e-4 * np.maximum(np.abs(J1), np.abs(J2)) + noise, axis=1)
 
 
-def _chain(J, t, cv):
+def _chain(J, t, cv, absolute=False):
     """d mag / d(s, q, rho, u1, u0, alpha, t0, tE) from the derivatives with
-    respect to (s, q, rho, u1, Re w, Im w), w on the rectilinear trajectory."""
+    respect to (s, q, rho, u1, Re w, Im w), w on the rectilinear trajectory
+    (absolute: the same map on magnitudes, for error bounds)."""
     u0, al, t0, te = cv[4], cv[5], cv[6], cv[7]
     tau = (t - t0) / te
     sa, ca = np.sin(al), np.cos(al)
+    cw = [(ca, -sa), (-u0 * sa + tau * ca, -u0 * ca - tau * sa), (-sa / te, -ca / te), (-tau * sa / te, -tau * ca / te)]
     jx, jy = J[:, 4], J[:, 5]
-    du0 = jx * ca - jy * sa
-    dal = jx * (-u0 * sa + tau * ca) + jy * (-u0 * ca - tau * sa)
-    dt0 = -(jx * sa + jy * ca) / te
-    dte = -tau * (jx * sa + jy * ca) / te
-    return np.stack([J[:, 0], J[:, 1], J[:, 2], J[:, 3], du0, dal, dt0, dte], axis=1)
+    f = np.abs if absolute else (lambda x: x)
+    cols = [f(a) * jx + f(b) * jy for a, b in cw]
+    return np.stack([J[:, 0], J[:, 1], J[:, 2], J[:, 3]] + cols, axis=1)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_vjp_full_length_curves_against_reference_differences(G, precision):
+    """The VJP of four whole curves against the reference's per-point central
+    differences (step 1e-7; points where the 1e-8 step disagrees, i.e. where a
+    discrete choice changed within +-h, get a zero cotangent): 1e-3 of the
+    cotangent-weighted L1 scale plus the differences' rounding noise."""
     d = G("vjp_seed3_fd")
     rng = np.random.default_rng(12)
     for c in d["curve_ids"]:
         t, cv, J = d[f"t{c}"], d[f"curve{c}"], d[f"jac{c}"]
-        ok = _trusted(J[0], J[1])
-        assert ok.mean() > 0.8, (c, ok.mean())
+        noise = _fd_noise(d[f"mag{c}"], cv)
+        ok = _trusted(J[0], J[1], noise)
+        assert ok.mean() > 0.85, (c, ok.mean())
         cot = np.where(ok, rng.normal(size=len(t)), 0.0)
-        off = np.array([0, len(t)])
-        g, m = C.mag_lc_batched_vjp(off, t, cv[None, :], cot, precision=precision, **LC)
+        g, m = C.mag_lc_batched_vjp(np.array([0, len(t)]), t, cv[None, :], cot, precision=precision, **LC)
         g, m = g.cpu().numpy()[0], m.cpu().numpy()
         assert rel(m, d[f"mag{c}"]).max() < BOUND[precision]
-        D = _chain(J[1], t, cv)
+        D = _chain(J[0], t, cv)
         ref = cot @ D
-        scale = np.abs(cot) @ np.abs(D)
-        assert np.all(np.abs(g - ref) <= 1e-3 * scale + 1e-12), (c, g, ref, scale)
+        tol = 1e-3 * (np.abs(cot) @ np.abs(D)) + np.abs(cot) @ _chain(noise, t, cv, absolute=True)
+        assert np.all(np.abs(g - ref) <= tol), (c, g, ref, tol)
 
 
 def _ambiguous(z, w, lens):
@@ -197,16 +208,35 @@ def test_lens_polynomial_matches_reference_coefficients(G):
         assert np.max(np.abs(c - ref)) <= 1e-12 * np.max(np.abs(ref))
 
 
+def _min_mass_fraction(q1, q2):
+    e1 = q1 / (1 + q1 + q2)
+    return np.minimum(np.minimum(e1, q1 * e1), 1 - e1 - q1 * e1)
+
+
+def test_triple_mixed_precision_routes_small_masses_to_fp64():
+    """Where a mass fraction is below 1e-2, FP32 cannot separate the images
+    clustered around that lens; the magnification kernels then run the FP64
+    solver under "mixed" and return the FP64 result exactly."""
+    s1, s2, q1, q2, psi, w = triple_workload()
+    for k in np.flatnonzero(_min_mass_fraction(q1, q2) < 1e-2)[:50]:
+        p = dict(s=s1[k], q=q1[k], q3=q2[k], r3=s2[k], psi=psi[k])
+        m32 = C.mag_point_source(w[k], nlenses=3, precision="mixed", **p)
+        m64 = C.mag_point_source(w[k], nlenses=3, precision="fp64", **p)
+        assert np.array_equal(m32, m64, equal_nan=True), k
+
+
 def test_triple_mixed_solver_against_fp64_full_workload():
-    """All 10^6 positions of the triple workload: the mixed solver (FP32
-    Aberth, compensated double-float stage, FP64 Newton polish) against the FP64
-    solver on the same polynomials (coefficients from cgb_lens_polynomial):
-    roots as sets (relative distance within root_bound), image counts equal
-    outside the ambiguous band, magnifications within the promised 1e-4."""
+    """Every position of the triple workload's systems whose mass fractions
+    all reach 1e-2 (those that keep the mixed solver; the others go to FP64,
+    above): the mixed solver (FP32 Aberth, compensated double-float stage,
+    FP64 Newton polish) against the FP64 solver on the same polynomials
+    (coefficients from cgb_lens_polynomial): roots as sets (relative distance
+    within root_bound), image counts equal outside the ambiguous band,
+    magnifications within the promised 1e-4."""
     s1, s2, q1, q2, psi, w = triple_workload()
     dev = torch.device("cuda", 0)
     worst_mu, mismatch = 0.0, 0
-    for k in range(1000):
+    for k in np.flatnonzero(_min_mass_fraction(q1, q2) >= 1e-2):
         p = dict(s=s1[k], q=q1[k], q3=q2[k], r3=s2[k], psi=psi[k])
         c = C.lens_polynomial(torch.as_tensor(w[k], device=dev), nlenses=3, **p)
         z64 = C.ehrlich_aberth(c, None, itmax=2500, precision="fp64").reshape(-1, 10).cpu().numpy()
