@@ -466,7 +466,7 @@ def extras_triple(C, dev, stream, nsys=1000, npos=1000):
             return res, torch.where(res < 1e-6, 1.0 / det.abs(), torch.zeros_like(det)).sum(1)
         r64, mu64 = filt(z64)
         r32, mu32 = filt(z32)
-        amb = ((r64 > 1e-6 / 30) & (r64 < 1e-6 * 30)).any(1)
+        amb = ((r64 > 1e-6 / 30) & (r64 < 1e-6 * 30)).any(1) | ((r32 > 1e-6 / 30) & (r32 < 1e-6 * 30)).any(1)
         mismatch += int((((r64 < 1e-6).sum(1) != (r32 < 1e-6).sum(1)) & ~amb).sum())
         worst_mu = max(worst_mu, float(((mu32 - mu64).abs() / mu64)[~amb].max()))
     n, nm = nsys * npos, len(mixed_sys) * npos
