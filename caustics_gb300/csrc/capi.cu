@@ -137,7 +137,7 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
   P.ld_group = (o->ld_group == 2 || o->ld_group == 4 || o->ld_group == 8) ? o->ld_group : 1;
   if (o->cta_threads != 0 && o->cta_threads != 64 && o->cta_threads != 128 && o->cta_threads != 256)
     return fail(CGB_ERR_INVALID, "cta_threads must be 0, 64, 128 or 256%s");
-  P.threads = o->cta_threads > 0 ? o->cta_threads : 256;
+  P.threads = o->cta_threads;  // 0: chosen at launch (launch_es_variant)
   if (o->labelling != 0 && o->labelling != 1) return fail(CGB_ERR_INVALID, "labelling must be 0 or 1%s");
   P.nearest = o->labelling;
   {

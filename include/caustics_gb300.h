@@ -82,9 +82,10 @@ typedef struct cgb_es_options {
                              off; 2 = the same test with the third lens where the lens equation puts it (r3)
                              and f'' = -2 sum eps_j/(z - r_j)^3 */
   int32_t cta_threads;    /* threads per contour-kernel CTA (one CTA per extended-source evaluation):
-                             64, 128 or 256, 0 = 256; fewer threads let more evaluations share an SM
-                             where shared memory allows (the phases run on few threads at small
-                             npts_limb); a launch-shape knob that changes no result */
+                             64, 128 or 256; 0 = automatic (128 for the forward at npts_limb <= 256,
+                             else 256); fewer threads let more evaluations share an SM where shared
+                             memory allows (the phases run on few threads at small npts_limb); a
+                             launch-shape knob that changes results only in the summation order */
 } cgb_es_options;
 
 /* Parameters of one binary-lens light curve for the batched entry points: lens
