@@ -61,11 +61,17 @@ def f_es(L, G):
     return L * 5.7e3 + 3.1 * L * G * 2 * 60
 
 
-# DRAM bytes (read + write) per contour evaluation of es_kernel<2, MIXED>
-# (instructions, constants, spills; the inputs are 24 B per point), from an ncu
-# capture of a contour-kernel launch (profiles/), scaled by the evaluations of a
-# launch
-DRAM_BYTES_PER_EVAL = 1.397e6 / 300
+# Per contour evaluation of es_kernel<2, MIXED> (npts_limb 200, npts_ld 100),
+# from one ncu capture of a contour-kernel launch (profiles/), divided by the
+# evaluations of that launch: DRAM bytes read + written (instructions,
+# constants, spills; the inputs are 24 B per point), and the executed FP64 and
+# FP32 arithmetic (dadd + dmul + 2 dfma, fadd + fmul + 2 ffma thread
+# instructions).
+NCU_EVALS = 2764
+DRAM_BYTES_PER_EVAL = 1.970e6 / NCU_EVALS
+FP64_FLOP_PER_EVAL = 1.4945e9 / NCU_EVALS
+FP32_FLOP_PER_EVAL = 2.3547e10 / NCU_EVALS
+FP64_PIPE_BUSY_NCU = 0.515
 
 
 def draw_batched(ncurves_total, seed, nmin, nmax, take):
@@ -241,6 +247,18 @@ def timed(stream, fn, reps=1, flush=None):
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
     return float(np.mean(ms))
+
+
+def _counted(nfull, ms, peaks):
+    """The contour evaluations' executed arithmetic (ncu counts per evaluation)
+    at the measured rate, against the live FMA peaks of each pipe."""
+    f64 = FP64_FLOP_PER_EVAL * nfull / (ms * 1e-3) / 1e12
+    f32 = FP32_FLOP_PER_EVAL * nfull / (ms * 1e-3) / 1e12
+    return {"fp64_flop_per_eval": FP64_FLOP_PER_EVAL, "fp32_flop_per_eval": FP32_FLOP_PER_EVAL,
+            "fp64_tflops": f64, "fp64_frac": f64 / peaks["fp64"], "fp32_tflops": f32, "fp32_frac": f32 / peaks["fp32"],
+            "fp64_pipe_busy_ncu": FP64_PIPE_BUSY_NCU,
+            "source": "ncu thread-instruction counters (dadd, dmul, dfma; fadd, fmul, ffma) of one es_kernel<2,MIXED> "
+                      "launch over the evaluations it ran (profiles/); contour evaluations only"}
 
 
 def fma_peaks(dev, stream):
@@ -506,7 +524,9 @@ def main():
         t0 = time.perf_counter()
         g, _ = C.mag_lc_batched_vjp(off, t, cv, cot, precision="mixed", **LC)
         torch.cuda.synchronize()
-        print(json.dumps({"only_vjp": True, "points": len(t), "s": time.perf_counter() - t0,
+        s = time.perf_counter() - t0
+        _, route = C.mag_lc_batched(off, t, cv, precision="mixed", return_route=True, **LC)  # after the VJP's launches
+        print(json.dumps({"only_vjp": True, "points": len(t), "full_contour_points": int(route.sum().item()), "s": s,
                           "grad_finite": bool(torch.isfinite(g).all())}))
         return
     if args.quick:
@@ -568,6 +588,7 @@ def main():
                      "peak_source": "measured live in bench.py (csrc/bench/probe_fma.cu, FP32 FMA burst); the path "
                                     "moves 24 B per point, so neither the HBM nor the tensor peak bounds it",
                      "fp64_fma_peak": peaks["fp64"],
+                     "counted": _counted(nfull, total_ms, peaks),
                      "hbm_sanity": {"bytes_per_point": 24,
                                     "achieved_gbs": 24 * npoints / (total_ms * 1e-3) / 1e9,
                                     "peak_gbs_measured": _measured_peaks().get("hbm_gbs")}},

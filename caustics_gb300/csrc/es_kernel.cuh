@@ -882,6 +882,46 @@ __device__ __forceinline__ void split_point_grad(double a, double b, double rho,
   }
 }
 
+// The lens as the FP64 recomputation below needs it, passed by value so the
+// caller's item stays in registers.
+template <int NL>
+struct NodeLens {
+  cd r[NL];
+  double eps[NL];
+};
+
+// 1 - |s/rho|^2 at one node in FP64, at the FP64 quadrature's node position
+// d = hw t + mid (relative to the contour point), with the FP64 quadrature's
+// arithmetic.  Where a node lies near a crossing of the limb, 1 - r^2 is a
+// difference of O(|s/rho - uc|) terms that nearly cancel; its FP32 rounding
+// (~1e-7 of those terms) then reaches the value itself, and dB/dr ~
+// 1/sqrt(1 - r^2) amplifies it without bound (measured: a node 1.3e-8 inside
+// the limb gave the wrong sign in FP32 and a per-point gradient off by 100 %).
+template <int NL>
+__device__ __noinline__ float limb_gap_fp64(NodeLens<NL> L, cd zc, cd w0, double rho, double d, int isQ) {
+  const double inv_rho = 1.0 / rho;
+  cd w = zc;
+#pragma unroll
+  for (int k = 0; k < NL; ++k) w = w - crecip(conj(zc) - conj(L.r[k])) * L.eps[k];
+  const cd uc = (w - w0) * inv_rho;
+  const double c1 = 1.0 - (uc.x * uc.x + uc.y * uc.y);
+  const cd cdl = isQ ? mk(d, 0.0) : mk(0.0, -d);
+  cd dl = isQ ? mk(d * inv_rho, 0.0) : mk(0.0, d * inv_rho);
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    const cd D = conj(zc) - conj(L.r[k]);
+    dl = dl + cdl * crecip(D + cdl) * crecip(D) * (L.eps[k] * inv_rho);
+  }
+  return (float)(c1 - 2.0 * (uc.x * dl.x + uc.y * dl.y) - (dl.x * dl.x + dl.y * dl.y));
+}
+
+// FP32 nodes recompute 1 - r^2 in FP64 where |1 - r^2| < X1_COND (|dl| + |dl|^2),
+// i.e. where its FP32 rounding (bounded by ~8 eps32 (|dl| + |dl|^2)) exceeds
+// 1e-3 of it.  On the gradient workload's worst evaluations that flags ~3.5e-4
+// of the nodes and leaves each line integral of dB within ~2e-5 of FP64
+// (CPU emulation of this arithmetic on the reference's contours).
+constexpr float X1_COND = 1e3f * 8.0f * 5.9604645e-8f;
+
 template <int NL, typename R, typename C>
 __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad<GradDirs<NL>::NK> &g,
                            const float (*glf)[2][GL_MAX]) {
@@ -943,7 +983,20 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
           dl = dl + cdl * u[k] * iDj[k] * (ej[k] * irho);
         }
         const C srho = C{uc.x + dl.x, uc.y + dl.y};
-        const R x1 = c1 - (R)2 * (uc.x * dl.x + uc.y * dl.y) - (dl.x * dl.x + dl.y * dl.y);  // 1 - r^2
+        R x1 = c1 - (R)2 * (uc.x * dl.x + uc.y * dl.y) - (dl.x * dl.x + dl.y * dl.y);  // 1 - r^2
+        if constexpr (sizeof(R) == sizeof(float)) {
+          const float dln = fabsf(dl.x) + fabsf(dl.y);
+          if (fabsf(x1) < X1_COND * dln * (1.0f + dln)) {
+            NodeLens<NL> nl;
+#pragma unroll
+            for (int k = 0; k < NL; ++k) {
+              nl.r[k] = It.L.r[k];
+              nl.eps[k] = It.L.eps[k];
+            }
+            const double d64 = fma(0.5 * ((hi - b) - (lo - b)), P.gl_x[half][j], 0.5 * ((hi - b) + (lo - b)));
+            x1 = limb_gap_fp64<NL>(nl, zc, It.w0, rho, d64, isQ);
+          }
+        }
         const R r = cabs(srho);
         R B, dB;
         if (x1 >= (R)0) {

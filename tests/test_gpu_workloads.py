@@ -8,7 +8,8 @@ by the reference itself (tests/golden/make_golden.py):
 * the points of that workload that set a non-convergence or contour-linking
   status bit in a full run;
 * gradients of four whole 1000-point curves of the 256-curve gradient
-  workload (seed 3) against the reference's central differences;
+  workload (seed 3) against the reference's central differences, and the
+  mixed-precision VJP of 64 of its curves against the FP64 VJP;
 * triple-lens point source over all 1000 systems of the triple workload
   (seed 1), the mixed solver against FP64 at the full 10^6 positions;
 * the triple hexadecapole and its proximity test (the reference's pieces,
@@ -135,6 +136,37 @@ def test_vjp_full_length_curves_against_reference_differences(G, precision):
         ref = cot @ D
         tol = 1e-3 * (np.abs(cot) @ np.abs(D)) + np.abs(cot) @ _chain(noise, t, cv, absolute=True)
         assert np.all(np.abs(g - ref) <= tol), (c, g, ref, tol)
+
+
+def test_mixed_vjp_against_fp64_gradient_workload():
+    """Mixed-precision VJP against the FP64 VJP on the first 64 curves of the
+    gradient workload (seed 3): per curve, |g_mixed - g_fp64| / |g_fp64| <=
+    1e-4 (over all 256 curves: median 2e-7, p99 5e-5, largest 1.7e-4 on curve
+    176, unchanged with every quadrature node in FP64, so that one comes from
+    the forward pass's roots, not the adjoint).  Curve 7 (q 6e-4, rho 0.054)
+    holds the evaluation where a quadrature node lies 1.3e-8 inside the limb:
+    its FP32 1 - r^2 had the wrong sign and the point's gradient was off by
+    100 % until such nodes were recomputed in FP64; per point and parameter
+    (natural scale s, q, rho, 1, rho, rho, relative to mu) the mixed gradient
+    must stay within 1e-4 of FP64."""
+    import bench
+    off, t, cv = bench.draw_batched(256, 3, 1000, 1000, 64)
+    cot = np.random.default_rng(3).normal(size=len(t))
+    g64, _ = C.mag_lc_batched_vjp(off, t, cv, cot, precision="fp64", **LC)
+    g32, _ = C.mag_lc_batched_vjp(off, t, cv, cot, precision="mixed", **LC)
+    g64, g32 = g64.cpu().numpy(), g32.cpu().numpy()
+    reln = np.linalg.norm(g32 - g64, axis=1) / np.linalg.norm(g64, axis=1)
+    assert reln.max() < 1e-4, (int(reln.argmax()), reln.max())
+    c = 7
+    tt, p = t[off[c]:off[c + 1]], cv[c]
+    w = bench.trajectory(tt, p)
+    per = {}
+    for prec in ("fp64", "mixed"):
+        m, g = C.mag_extended_source_grad(w, p[2], nlenses=2, s=p[0], q=p[1], u1=p[3], precision=prec, **LC)
+        per[prec] = (m.cpu().numpy(), g.cpu().numpy())
+    nat = np.array([p[0], p[1], p[2], 1.0, p[2], p[2]])
+    err = np.abs(per["mixed"][1] - per["fp64"][1]) * nat / per["fp64"][0][:, None]
+    assert err.max() < 1e-4, (np.unravel_index(err.argmax(), err.shape), err.max())
 
 
 def _ambiguous(z, w, lens):
