@@ -466,7 +466,7 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
     for binary lenses, grad [n, 9] with d mag / d(q3, r3, psi) appended for
     triple lenses: the hand-written adjoint of mag_extended_source.
     grad_fp64_above: in "mixed", contour points whose image tangents exceed it
-    run the adjoint quadrature in FP64 (0 = default, < 0 = all)."""
+    run the adjoint quadrature in FP64 (0 = default 6, < 0 = all)."""
     wt, was_np = _to_device(np.atleast_1d(w0) if np.ndim(w0) == 0 and not isinstance(w0, torch.Tensor) else w0,
                             torch.complex128)
     wf = wt.reshape(-1).contiguous()

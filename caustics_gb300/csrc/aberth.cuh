@@ -386,10 +386,15 @@ __device__ bool aberth64_group(const cd (&p)[DEG + 1], cd &zr, int itmax, unsign
   return false;
 }
 
-// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
-// correction is at most 2^-40 |z|.
+// FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
+// correction is at most 2^-40 |z|.  With sep2 = S^2 (default: infinite, the
+// plain rule only), S = sum_{k != j} 1/|z - z_k|
+// over the other roots, a step is also final when Newton's error model puts
+// the next correction, |c|^2 |p''/(2p')| = |c|^2 |sum_k 1/(z - z_k)| <= |c|^2 S,
+// at most 2^-40 |z|: from an FP32 root (relative error ~1e-7) one step then
+// leaves ~1e-13, where the plain rule needs a second step to see it.
 template <int DEG, int SWEEPS = 3>
-__device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
+__device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z, float sep2 = INFINITY) {
   for (int sweep = 0; sweep < SWEEPS; ++sweep) {
     cd h = p[DEG], hd = mk(0, 0);
 #pragma unroll
@@ -399,9 +404,24 @@ __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
     }
     const cd c = cdiv(h, hd);
     z = z - c;
-    if (norm2(c) <= 8.271806125530277e-25 * fmax(norm2(z), 1e-300)) return true;
+    const double c2 = norm2(c), z2 = 8.271806125530277e-25 * fmax(norm2(z), 1e-300);
+    if (c2 <= z2 || c2 * c2 * (double)sep2 <= z2) return true;
   }
   return false;
+}
+
+// S_j^2, S_j = sum_{k != j} 1/|z_j - z_k| (FP32), for newton_polish_root's
+// error model; infinite for coincident roots, which then never stop early.
+template <int DEG>
+__device__ __forceinline__ void root_separation2(const cf (&z)[DEG], float (&s2)[DEG]) {
+#pragma unroll
+  for (int j = 0; j < DEG; ++j) {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < DEG; ++k)
+      if (k != j) s += rsqrtf(norm2(z[j] - z[k]));
+    s2[j] = s * s;
+  }
 }
 
 // Mixed precision: FP32 Aberth, FP32 compensated stage against the double-float
@@ -413,7 +433,10 @@ __device__ bool newton_polish_root(const cd (&p)[DEG + 1], cd &z) {
 // one-polynomial-per-thread kernels, where a warp waits for its slowest lane;
 // in the contour kernel it measured slower (the chained matching that follows
 // ran 50 % longer with that code present), so that kernel starts cold.
-template <int DEG, bool WARM_FALLBACK = false>
+// EARLY: each root's polish may stop after one step on newton_polish_root's
+// error model (roots to ~1e-13 instead of ~1e-16; the contour kernel's limb
+// solves, whose results need 1e-4); the point-source kernels keep the plain rule.
+template <int DEG, bool WARM_FALLBACK = false, bool EARLY = false>
 __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm, uint32_t &flags) {
   cf ph[DEG + 1], pl[DEG + 1];
   float alpha[DEG + 1];
@@ -493,21 +516,44 @@ __device__ int aberth_mixed(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, boo
   // correction is at most 2^-40 |z| (compared without a division; a NaN
   // correction never passes)
   bool conv = false;
-  for (int sweep = 0; sweep < 3 && ok; ++sweep) {
-    conv = true;
+  if constexpr (EARLY) {
+    float s2[DEG];
+    root_separation2<DEG>(zf, s2);
+    uint32_t done = 0;
+    for (int sweep = 0; sweep < 3 && ok && done != all; ++sweep) {
 #pragma unroll
-    for (int j = 0; j < DEG; ++j) {
-      cd h = p[DEG], hd = mk(0, 0);
+      for (int j = 0; j < DEG; ++j) {
+        if ((done >> j) & 1u) continue;
+        cd h = p[DEG], hd = mk(0, 0);
 #pragma unroll
-      for (int k = DEG - 1; k >= 0; --k) {
-        hd = cfma(hd, z[j], h);
-        h = cfma(h, z[j], p[k]);
+        for (int k = DEG - 1; k >= 0; --k) {
+          hd = cfma(hd, z[j], h);
+          h = cfma(h, z[j], p[k]);
+        }
+        const cd c = cdiv(h, hd);
+        z[j] = z[j] - c;
+        const double c2 = norm2(c), z2 = 8.271806125530277e-25 * fmax(norm2(z[j]), 1e-300);
+        if (c2 <= z2 || c2 * c2 * (double)s2[j] <= z2) done |= 1u << j;
       }
-      cd c = cdiv(h, hd);
-      z[j] = z[j] - c;
-      conv = conv && norm2(c) <= 8.271806125530277e-25 * fmax(norm2(z[j]), 1e-300);
     }
-    if (conv) break;
+    conv = done == all;
+  } else {
+    for (int sweep = 0; sweep < 3 && ok; ++sweep) {
+      conv = true;
+#pragma unroll
+      for (int j = 0; j < DEG; ++j) {
+        cd h = p[DEG], hd = mk(0, 0);
+#pragma unroll
+        for (int k = DEG - 1; k >= 0; --k) {
+          hd = cfma(hd, z[j], h);
+          h = cfma(h, z[j], p[k]);
+        }
+        cd c = cdiv(h, hd);
+        z[j] = z[j] - c;
+        conv = conv && norm2(c) <= 8.271806125530277e-25 * fmax(norm2(z[j]), 1e-300);
+      }
+      if (conv) break;
+    }
   }
   ok = ok && conv;
   // distinct roots (Newton alone may merge a near-double pair)

@@ -141,10 +141,13 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
   if (o->labelling != 0 && o->labelling != 1) return fail(CGB_ERR_INVALID, "labelling must be 0 or 1%s");
   P.nearest = o->labelling;
   {
-    // default 2: on 64 random light curves x 1000 points the mixed VJP then
-    // matches the all-FP64 adjoint's agreement with finite differences, at
-    // 2.6x its speed (threshold 8: 4x faster, but 8e-4 from the FP64 gradient)
-    const double a = o->grad_fp64_above == 0.0 ? 2.0 : o->grad_fp64_above;
+    // default 6: on the 256 x 1000-point gradient workload, thresholds 2, 3,
+    // 4, 6 and 8 took 637, 494, 425, 355 and 327 ms per 64 curves; the largest
+    // per-curve difference to the FP64 VJP over the first 64 curves was 1.4e-5,
+    // 4.0e-5, 3.2e-5, 2.6e-5 and 1.1e-4 (over all 256: 1.7e-4 at every threshold,
+    // from the forward pass of one curve).  Before FP32 nodes near a limb
+    // crossing recomputed 1 - r^2 in FP64, threshold 8 was 8e-4 off.
+    const double a = o->grad_fp64_above == 0.0 ? 6.0 : o->grad_fp64_above;
     P.grad_amp2 = a < 0.0 ? -1.0 : a * a;
   }
   P.qchunk = o->queue_chunk > 0 ? o->queue_chunk : 1;

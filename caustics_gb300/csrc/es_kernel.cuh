@@ -247,7 +247,11 @@ static __device__ void bitonic_sort_desc(long long *v, uint16_t *ix, int n) {
   __syncthreads();
 }
 
-template <int NL, int PREC>
+// EARLY: the mixed solver's polish may stop after one step (aberth_mixed);
+// the forward kernels take it, the adjoint keeps full FP64 roots (its image
+// tangents ~1/det J amplify root errors near critical curves: 1e-13 roots
+// moved a curve's gradient by 1e-3)
+template <int NL, int PREC, bool EARLY = false>
 __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, cd *zrow, const cd *warm,
                                  uint16_t &mkb, uint16_t &pp, uint16_t &zp, uint32_t &flags) {
   constexpr int DEG = NL * NL + 1;
@@ -260,7 +264,7 @@ __device__ void solve_limb_point(const EsParams &P, const EsItem &I, double th, 
 #pragma unroll
     for (int i = 0; i < DEG; ++i) z[i] = warm[i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
   }
-  int it = (PREC == MIXED) ? aberth_mixed<DEG, true>(p, z, P.itmax, warm != nullptr, flags)
+  int it = (PREC == MIXED) ? aberth_mixed<DEG, true, EARLY>(p, z, P.itmax, warm != nullptr, flags)
                            : aberth64<DEG>(p, z, P.itmax, warm != nullptr);
   if (it < 0) flags |= CGB_ST_NOCONV;
   mkb = 0;
@@ -917,10 +921,11 @@ __device__ __noinline__ float limb_gap_fp64(NodeLens<NL> L, cd zc, cd w0, double
 
 // FP32 nodes recompute 1 - r^2 in FP64 where |1 - r^2| < X1_COND (|dl| + |dl|^2),
 // i.e. where its FP32 rounding (bounded by ~8 eps32 (|dl| + |dl|^2)) exceeds
-// 1e-3 of it.  On the gradient workload's worst evaluations that flags ~3.5e-4
-// of the nodes and leaves each line integral of dB within ~2e-5 of FP64
-// (CPU emulation of this arithmetic on the reference's contours).
-constexpr float X1_COND = 1e3f * 8.0f * 5.9604645e-8f;
+// 1e-2 of it: ~3e-5 of the nodes on the gradient workload's worst evaluations
+// (CPU emulation of this arithmetic on the reference's contours).  Measured on
+// that workload: thresholds 3x and 10x higher left every per-point gradient
+// difference to FP64 the same to three digits and cost 1.6 % and 5 % more time.
+constexpr float X1_COND = 1e2f * 8.0f * 5.9604645e-8f;
 
 template <int NL, typename R, typename C>
 __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad<GradDirs<NL>::NK> &g,
@@ -1349,7 +1354,7 @@ __device__ __forceinline__ double limb_theta(int k, int n0) {
 // same deterministic solver), whose roots are the raw rows to order.
 // Items are enumerated exactly as the contour kernel takes them.
 constexpr int FO_THREADS = 128;
-template <int NL, int PREC>
+template <int NL, int PREC, bool EARLY>
 __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                                    const int64_t *__restrict__ index,
                                                                    const uint8_t *__restrict__ route,
@@ -1371,7 +1376,7 @@ __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsPara
       cd z[DEG];
       uint16_t mkb, pp, zp;
       uint32_t flags = 0;
-      solve_limb_point<NL, PREC>(P, I, th, z, nullptr, mkb, pp, zp, flags);
+      solve_limb_point<NL, PREC, EARLY>(P, I, th, z, nullptr, mkb, pp, zp, flags);
 #pragma unroll
       for (int i = 0; i < DEG; ++i) zs[g][i] = z[i];
     }
@@ -1521,7 +1526,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
       const double th = limb_theta(k, n0);
       S.TH[k] = th;
       S.ORD[k] = (uint16_t)k;
-      solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)k * DEG, nullptr, S.MK[k], S.PP[k], S.ZP[k], flags);
+      solve_limb_point<NL, PREC, !GRAD>(P, I, th, S.Z + (size_t)k * DEG, nullptr, S.MK[k], S.PP[k], S.ZP[k], flags);
     }
     if (P.dbg && lane == 0) dbg_arr[warp] = clock64();
     __syncthreads();
@@ -1781,7 +1786,18 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
               if (__all_sync(gmask, done)) break;
             }
             const bool ok = __all_sync(gmask, done && isfinite(zr.x) && isfinite(zr.y));
-            if (lg < DEG) S.Z[(size_t)slot * DEG + lg] = tod(zr);
+            // S^2 of this root for the polish's error model (newton_polish_root),
+            // handed over in the point's flag slots
+            float sep = 0.0f;
+#pragma unroll
+            for (int q = 0; q < DEG; ++q) {
+              const cf zq = mkf(__shfl_sync(gmask, zr.x, q, FG), __shfl_sync(gmask, zr.y, q, FG));
+              if (q != lg) sep += rsqrtf(norm2(zr - zq));
+            }
+            if (lg < DEG) {
+              S.Z[(size_t)slot * DEG + lg] = tod(zr);
+              rflag[(size_t)j * DEG + lg] = __float_as_uint(sep * sep);
+            }
             if (lg == 0) {
               pok[j] = ok ? 1 : 0;
               if (P.dbg) {
@@ -1807,7 +1823,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
 #pragma unroll
             for (int q = 0; q <= DEG; ++q) p[q] = pco[(size_t)j * (DEG + 2) + q];
             cd z = S.Z[(size_t)slot * DEG + i];
-            if (newton_polish_root<DEG, 5>(p, z)) f |= 1u;
+            if (newton_polish_root<DEG, 5>(p, z, GRAD ? INFINITY : __uint_as_float(rflag[idx]))) f |= 1u;
             S.Z[(size_t)slot * DEG + i] = z;
             double r, d;
             lens_filter<NL>(I.L, z, pco[(size_t)j * (DEG + 2) + DEG + 1], r, d);
@@ -1963,7 +1979,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
         S.TH[slot] = th;
         // warm start from the left neighbour's rows (extended_source.py:79-98,
         // 128-129); the row order is the reference's warm-start labelling
-        solve_limb_point<NL, PREC>(P, I, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
+        solve_limb_point<NL, PREC, !GRAD>(P, I, th, S.Z + (size_t)slot * DEG, S.Z + (size_t)sl * DEG, S.MK[slot],
                                    S.PP[slot], S.ZP[slot], flags);
         bool amb;
         const uint64_t m = step_map<DEG>(S.Z + (size_t)sl * DEG, S.Z + (size_t)slot * DEG, amb);
@@ -2436,7 +2452,7 @@ cudaError_t launch_es_variant(const EsParams &P, const cd *w0, const int64_t *in
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    es_first_order_kernel<NL, PREC><<<sms * 8, FO_THREADS, 0, stream>>>(P, w0, index, route, n,
+    es_first_order_kernel<NL, PREC, !GRAD><<<sms * 8, FO_THREADS, 0, stream>>>(P, w0, index, route, n,
                                                                          const_cast<uint64_t *>(P.perm0));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -73,7 +73,7 @@ typedef struct cgb_es_options {
                              bench light curve) */
   double grad_fp64_above; /* mixed-precision adjoints: a contour point whose image tangents |dz/dtheta|
                              (own or neighbours', ~1/|det J|) exceed this runs its limb-darkening
-                             quadrature in FP64; 0 = default (2), < 0 = every point in FP64 */
+                             quadrature in FP64; 0 = default (6), < 0 = every point in FP64 */
   int32_t triple_routing; /* cgb_mag with triple lenses: 0 = contour integral at every point, as the
                              reference's mag() (src/caustics/lightcurve.py:226-227); 1 = the reference's
                              triple hexadecapole (src/caustics/multipole.py:220-229) and the triple branch of its

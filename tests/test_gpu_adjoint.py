@@ -80,6 +80,11 @@ def fd_stable(w, rho, s, q, u1, npts, nld, ld, k):
     return f2, ok
 
 
+def PSCALE(s, q, rho):
+    """Natural scales of (s, q, rho, u1, Re w, Im w)."""
+    return np.array([s, q, rho, 1.0, rho, rho])
+
+
 CASES = [  # (points, rho, s, q, u1, npts_limb, npts_ld, limb darkening)
     ("near caustic, LD", 1e-2, 0.9, 0.2, 0.7, 300, 100, True),
     ("near caustic, uniform", 1e-2, 0.9, 0.2, 0.0, 300, 100, False),
@@ -107,7 +112,13 @@ def test_adjoint_vs_central_differences(G, case, prec):
             continue
         f, ok = fd_stable(w, rho, s, q, u1, npts, nld, ld, k)
         scale = np.maximum(np.abs(f), 1e-3 * mag)
-        err = np.abs(g[:, k] - f) / scale
+        # mixed precision differentiates its own forward pass, whose FP32
+        # quadrature sits ~1e-8 of mu from FP64's; through the 2 mu / rho term
+        # of d mu / d rho (and alike) that allows 1e-6 of mu on the parameter's
+        # natural scale (measured: 1.8e-7 at w = 0.6 + 0.4i, where d mu / d rho
+        # is 2e4 times smaller than 2 mu / rho)
+        floor = 1e-6 * mag / PSCALE(s, q, rho)[k] if prec == 1 else 0.0
+        err = np.maximum(np.abs(g[:, k] - f) - floor, 0.0) / scale
         checked += ok.sum()
         assert np.all(err[ok] < 1e-3), (NAMES[k], g[ok, k], f[ok])
     assert checked >= 6 * len(w) // 2

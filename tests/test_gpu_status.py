@@ -120,8 +120,9 @@ def test_repeated_calls_are_bit_identical():
         f2 = C.mag_lc_batched(off, t, cv, precision=prec, **LC)
         assert torch.equal(f1, f2)
         # the adjoint's forward runs in another kernel instantiation (its own
-        # instruction scheduling of the same arithmetic)
-        assert torch.allclose(f1, m1, rtol=1e-12, atol=0)
+        # instruction scheduling), and in mixed precision it polishes every root
+        # to full FP64 accuracy where the forward kernels may stop at ~1e-13
+        assert torch.allclose(f1, m1, rtol=1e-12 if prec == "fp64" else 1e-10, atol=0)
     w = rng.uniform(-0.2, 0.2, 16) + 1j * rng.uniform(-0.2, 0.2, 16)
     a = C.mag_extended_source_grad(w, 1e-2, s=1.1, q=5e-3, u1=0.5, precision="mixed", **LC)
     b = C.mag_extended_source_grad(w, 1e-2, s=1.1, q=5e-3, u1=0.5, precision="mixed", **LC)
