@@ -68,10 +68,17 @@ def f_es(L, G):
 # FP32 arithmetic (dadd + dmul + 2 dfma, fadd + fmul + 2 ffma thread
 # instructions).
 NCU_EVALS = 2764
-DRAM_BYTES_PER_EVAL = 1.970e6 / NCU_EVALS
-FP64_FLOP_PER_EVAL = 1.4945e9 / NCU_EVALS
-FP32_FLOP_PER_EVAL = 2.3547e10 / NCU_EVALS
-FP64_PIPE_BUSY_NCU = 0.515
+DRAM_BYTES_PER_EVAL = 5.601e6 / NCU_EVALS
+FP64_FLOP_PER_EVAL = 1.1711e9 / NCU_EVALS
+FP32_FLOP_PER_EVAL = 2.3639e10 / NCU_EVALS
+FP64_PIPE_BUSY_NCU = 0.573
+# the same for es_kernel<2, MIXED, GRAD> (the VJP's contour kernel), one
+# launch over 2000 contour evaluations of the gradient workload
+NCU_EVALS_VJP = 2000
+DRAM_BYTES_PER_EVAL_VJP = 55.24e6 / NCU_EVALS_VJP
+FP64_FLOP_PER_EVAL_VJP = 4.4575e9 / NCU_EVALS_VJP
+FP32_FLOP_PER_EVAL_VJP = 6.3113e10 / NCU_EVALS_VJP
+FP64_PIPE_BUSY_NCU_VJP = 0.706
 
 
 def draw_batched(ncurves_total, seed, nmin, nmax, take):
@@ -249,16 +256,19 @@ def timed(stream, fn, reps=1, flush=None):
     return float(np.mean(ms))
 
 
-def _counted(nfull, ms, peaks):
+def _counted(nfull, ms, peaks, vjp=False):
     """The contour evaluations' executed arithmetic (ncu counts per evaluation)
     at the measured rate, against the live FMA peaks of each pipe."""
-    f64 = FP64_FLOP_PER_EVAL * nfull / (ms * 1e-3) / 1e12
-    f32 = FP32_FLOP_PER_EVAL * nfull / (ms * 1e-3) / 1e12
-    return {"fp64_flop_per_eval": FP64_FLOP_PER_EVAL, "fp32_flop_per_eval": FP32_FLOP_PER_EVAL,
+    f64e, f32e, busy = ((FP64_FLOP_PER_EVAL_VJP, FP32_FLOP_PER_EVAL_VJP, FP64_PIPE_BUSY_NCU_VJP) if vjp else
+                        (FP64_FLOP_PER_EVAL, FP32_FLOP_PER_EVAL, FP64_PIPE_BUSY_NCU))
+    f64 = f64e * nfull / (ms * 1e-3) / 1e12
+    f32 = f32e * nfull / (ms * 1e-3) / 1e12
+    kern = "es_kernel<2,MIXED,GRAD>" if vjp else "es_kernel<2,MIXED>"
+    return {"fp64_flop_per_eval": f64e, "fp32_flop_per_eval": f32e,
             "fp64_tflops": f64, "fp64_frac": f64 / peaks["fp64"], "fp32_tflops": f32, "fp32_frac": f32 / peaks["fp32"],
-            "fp64_pipe_busy_ncu": FP64_PIPE_BUSY_NCU,
-            "source": "ncu thread-instruction counters (dadd, dmul, dfma; fadd, fmul, ffma) of one es_kernel<2,MIXED> "
-                      "launch over the evaluations it ran (profiles/); contour evaluations only"}
+            "fp64_pipe_busy_ncu": busy,
+            "source": f"ncu thread-instruction counters (dadd, dmul, dfma; fadd, fmul, ffma) of one {kern} launch over "
+                      "the evaluations it ran (profiles/); contour evaluations only"}
 
 
 def fma_peaks(dev, stream):
@@ -371,7 +381,8 @@ def vjp_line(C, dev, stream, flush, peaks, args):
             "mixed_vs_fp64_grad_max_rel_component": comp, "mixed_vs_fp64_grad_max_rel_norm_per_curve": norm,
             "bit_identical_repeat": bool(torch.equal(g32, g2)),
             "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": peaks["fp32"], "unit": "TFLOP/s",
-                         "frac": achieved / peaks["fp32"], "traffic": None,
+                         "frac": achieved / peaks["fp32"], "traffic": DRAM_BYTES_PER_EVAL_VJP * nfull,
+                         "counted": _counted(nfull, vms, peaks, vjp=True),
                          "flop_per_unit": "3 x forward: contour point 3 x 8.58e6, hexadecapole point 3 x 1.37e4",
                          "kernel": "cgb_mag_lc_batched_vjp (point pass, first-point ordering, es_kernel<2,MIXED,GRAD>, "
                                    "curve sums), CUDA events around the call",
