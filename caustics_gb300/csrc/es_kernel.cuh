@@ -760,17 +760,21 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst 
   const float cu = K.c0 * K.u1, cc = K.c0 * (1.0f - 2.0f * K.u1);
   cf uc;
   sincosf((float)th, &uc.y, &uc.x);
+  // D = conj(zc) - conj(r_j) in FP64 (an image near a lens makes it a small
+  // difference of O(1) numbers), then FP32 like the nodes: on GB300 every FP64
+  // instruction, conversions included, costs a warp the same ~64 cycles of its
+  // scheduler's FP64 pipe
   cf Dj[NL], Dj2[NL];
   float ej[NL];
 #pragma unroll
   for (int j = 0; j < NL; ++j) {
     const cd d = conj(zc) - conj(It.L.r[j]);
     Dj[j] = tof(d);
-    Dj2[j] = tof(d * d);
+    Dj2[j] = Dj[j] * Dj[j];
     ej[j] = K.ej[j];
   }
   const float irf = K.irf;
-  double acc[2] = {0.0, 0.0};
+  float acc[2] = {0.0f, 0.0f};
 #pragma unroll
   for (int isQ = 0; isQ < 2; ++isQ) {
     const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
@@ -812,11 +816,12 @@ __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst 
         s1 = fmaf(glf[half][1][j + jstep], fmaf(cu, brightness_bn_fast(n1), cc), s1);
       }
       if (j < n) s0 = fmaf(glf[half][1][j], fmaf(cu, brightness_bn_fast(node_n2(fmaf(hw, glf[half][0][j], mid))), cc), s0);
-      const float sum = s0 + s1;
-      acc[isQ] += (double)hw * (double)sum;
+      // FP32: the halves cancel by at most a factor 2 (the reference's split
+      // point a + |b - a| / 2 can lie beyond a when b < a)
+      acc[isQ] = fmaf(hw, s0 + s1, acc[isQ]);
     }
   }
-  return mk(-0.5 * acc[0], 0.5 * acc[1]);  // (P_i, Q_i)
+  return mk(-0.5 * (double)acc[0], 0.5 * (double)acc[1]);  // (P_i, Q_i)
 }
 
 
