@@ -1077,13 +1077,16 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
 }
 
 
-// Tangents dz/dtheta of an image z on the limb point of angle th, for the
-// parameter directions of GradDirs: from lens_eq(z) = w0 + rho e^{i th},
+// Tangents dz/dtheta of an image z of a limb point, for the parameter
+// directions of GradDirs: from lens_eq(z) = w0 + rho e^{i th},
 // dz = (g - lam conj(g)) / (1 - |lam|^2), lam = sum_j eps_j / (conj(z) - conj(r_j))^2,
 // g = the source-plane shift the parameter produces at fixed z (w0 and rho
 // move the source; the lens directions move the lens equation by -lens_shifts).
+// e^{i th} = (lens_eq(z) - w0) / rho comes from the reciprocals computed here
+// anyway (a few FP64 operations where sincos(th) takes tens; the image's
+// residual, ~1e-15, puts it within ~1e-15 / rho of the limb's value).
 template <int NL>
-__device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th, cd (&t)[GradDirs<NL>::NK]) {
+__device__ __forceinline__ void image_tangents(const EsItem &I, cd z, cd (&t)[GradDirs<NL>::NK]) {
   constexpr int NLD = GradDirs<NL>::NLENS;
   cd u[NL];
   double ej[NL];
@@ -1096,11 +1099,13 @@ __device__ __forceinline__ void image_tangents(const EsItem &I, cd z, double th,
 #pragma unroll
   for (int k = 1; k < NL; ++k) lam = lam + u[k] * u[k] * ej[k];
   const double iD = 1.0 / (1.0 - norm2(lam));
-  double sn, cs;
-  sincos(th, &sn, &cs);
+  cd e = z;
+#pragma unroll
+  for (int k = 0; k < NL; ++k) e = e - u[k] * ej[k];
+  e = (e - I.w0) * (1.0 / I.rho);
   cd dsl[NLD];
   lens_shifts<NL, double, cd>(u, ej, dsl);
-  cd g[4 + NLD] = {mk(cs, sn), mk(0.0, 0.0), mk(1.0, 0.0), mk(0.0, 1.0)};
+  cd g[4 + NLD] = {e, mk(0.0, 0.0), mk(1.0, 0.0), mk(0.0, 1.0)};
 #pragma unroll
   for (int m = 0; m < NLD; ++m) g[4 + m] = mk(-dsl[m].x, -dsl[m].y);
 #pragma unroll
@@ -1157,10 +1162,9 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
           // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
           // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
           cd tn[NK], tp[NK], ti[NK];
-          const uint32_t cpn = S.CP[in], cpp = S.CP[ip];
-          image_tangents<NL>(I, zn, S.TH[cpn / DEG], tn);
-          image_tangents<NL>(I, zp, S.TH[cpp / DEG], tp);
-          image_tangents<NL>(I, zc, S.TH[S.CP[i] / DEG], ti);
+          image_tangents<NL>(I, zn, tn);
+          image_tangents<NL>(I, zp, tp);
+          image_tangents<NL>(I, zc, ti);
           // Near a critical curve the tangents grow like 1/|det J| and the
           // pointwise contributions cancel in the sum; there the FP32 node values
           // (relative error ~1e-7) would be amplified, so such points run the
@@ -1228,7 +1232,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
       }
       const uint32_t cp = S.CP[i];
       cd t[NK];
-      image_tangents<NL>(I, S.Z[cp], S.TH[cp / DEG], t);
+      image_tangents<NL>(I, S.Z[cp], t);
 #pragma unroll
       for (int k = 0; k < NK; ++k) acc[k] += G.x * t[k].x + G.y * t[k].y;
     }
