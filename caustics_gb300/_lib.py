@@ -38,7 +38,8 @@ class EsOptions(ctypes.Structure):
                 ("npts_ld", ctypes.c_int32), ("roots_itmax", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("grid", ctypes.c_int32), ("queue_chunk", ctypes.c_int32), ("ld_group", ctypes.c_int32),
                 ("labelling", ctypes.c_int32), ("grad_fp64_above", ctypes.c_double),
-                ("triple_routing", ctypes.c_int32), ("cta_threads", ctypes.c_int32)]
+                ("triple_routing", ctypes.c_int32), ("cta_threads", ctypes.c_int32),
+                ("point_lanes", ctypes.c_int32)]
 
 
 class CurveParams(ctypes.Structure):

@@ -296,7 +296,7 @@ _TRIPLE_ROUTING = {"contour": 0, "reference": 1, "corrected": 2}
 
 
 def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid=0, queue_chunk=1, ld_group=1,
-                grad_fp64_above=0.0, labelling="reference", triple_routing="contour", cta_threads=0):
+                grad_fp64_above=0.0, labelling="reference", triple_routing="contour", cta_threads=0, point_lanes=0):
     if labelling not in _LABELLING:
         raise ValueError(f"labelling must be one of {sorted(_LABELLING)}")
     if triple_routing not in _TRIPLE_ROUTING:
@@ -304,7 +304,7 @@ def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, 
     return L.EsOptions(int(npts_limb), int(bool(limb_darkening)), float(u1), int(npts_ld), int(roots_itmax),
                        _precision(precision or "fp64"), int(grid), int(queue_chunk), int(ld_group),
                        _LABELLING[labelling], float(grad_fp64_above), _TRIPLE_ROUTING[triple_routing],
-                       int(cta_threads))
+                       int(cta_threads), int(point_lanes))
 
 
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
@@ -389,13 +389,13 @@ def _workspace(n, device, vjp=False):
 
 def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
                    precision="mixed", grid=0, queue_chunk=1, ld_group=1, return_route=False, return_status=False,
-                   out=None, labelling="reference", cta_threads=0):
+                   out=None, labelling="reference", cta_threads=0, point_lanes=0):
     """mag() for many binary-lens light curves of uneven lengths in one pass.
 
     offsets: int64 [ncurves+1]; t: float64 [npoints]; curves: float64
     [ncurves, 8] = (s, q, rho, u1, u0, alpha, t0, tE) per curve, the source on
     the rectilinear trajectory.  Per-curve u1 is used when limb_darkening.
-    grid, queue_chunk, ld_group, cta_threads: launch shape (autotune.tune)."""
+    grid, queue_chunk, ld_group, cta_threads, point_lanes: launch shape (autotune.tune)."""
     off, tt, cv = _batched_args(offsets, t, curves)
     n = tt.numel()
     dev = tt.device
@@ -408,7 +408,7 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
         mag_out, route, st, ws = out
         nbytes = ws.numel()
     opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
-                       labelling=labelling, cta_threads=cta_threads)
+                       labelling=labelling, cta_threads=cta_threads, point_lanes=point_lanes)
     with torch.cuda.device(dev):
         L.check(L.lib().cgb_mag_lc_batched(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
                                            _ptr(st), opts, _ptr(ws), nbytes, _stream()), "cgb_mag_lc_batched")
@@ -422,8 +422,10 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
 
 def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
                        precision="mixed", grid=0, queue_chunk=1, ld_group=1, grad_fp64_above=0.0,
-                       labelling="reference", cta_threads=0):
-    """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c]."""
+                       labelling="reference", cta_threads=0, point_lanes=0):
+    """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c].
+    point_lanes is accepted for symmetry with mag_lc_batched; the adjoint's
+    per-point pass takes one thread per point."""
     off, tt, cv = _batched_args(offsets, t, curves)
     ct, _ = _to_device(cot, torch.float64)
     n = tt.numel()

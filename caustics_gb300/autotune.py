@@ -6,7 +6,9 @@ Tunes, by timing candidates on (a sample of) the caller's workload:
   on at once, and how many evaluations share an SM;
 * the persistent grid of the contour kernel (occupancy-sized, or one CTA per SM);
 * the device work-queue chunk (items taken per queue grab);
-* the lanes that share one contour point's Gauss-Legendre nodes.
+* the lanes that share one contour point's Gauss-Legendre nodes;
+* threads per polynomial in the per-point pass (one thread per point, or a
+  group of 8 lanes with one lane per root), tried on the best shape found.
 Results are cached per (device, npts_limb, limb darkening, npts_ld, precision,
 labelling, workload size bucket, share of points on curves with q < 0.01): the
 last two decide how many evaluations reach the contour kernel and how uneven
@@ -18,7 +20,7 @@ import math
 import numpy as np
 import torch
 
-DEFAULT = dict(grid=0, queue_chunk=1, ld_group=1, cta_threads=0)
+DEFAULT = dict(grid=0, queue_chunk=1, ld_group=1, cta_threads=0, point_lanes=0)
 _CACHE = {}
 
 
@@ -61,7 +63,8 @@ def tune(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, r
         cands.append(dict(grid=0, queue_chunk=chunk, ld_group=group, cta_threads=threads))
     cands += [dict(grid=sms, queue_chunk=c, ld_group=g, cta_threads=256) for c, g in itertools.product((1, 2), (1, 2))]
     best, best_ms, table = None, float("inf"), []
-    for cfg in cands:
+
+    def trial(cfg):
         api.mag_lc_batched(so, st, sc, **kw, **cfg)
         ms = []
         for _ in range(reps):
@@ -73,8 +76,16 @@ def tune(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, r
             ms.append(e0.elapsed_time(e1))
         m = float(np.median(ms))
         table.append((cfg, m))
+        return m
+
+    for cfg in cands:
+        m = trial(dict(cfg, point_lanes=1))
         if m < best_ms:
-            best, best_ms = cfg, m
+            best, best_ms = dict(cfg, point_lanes=1), m
+    cfg = dict(best, point_lanes=8)
+    m = trial(cfg)
+    if m < best_ms:
+        best, best_ms = cfg, m
     if verbose:
         for cfg, m in table:
             print(cfg, f"{m:.3f} ms")

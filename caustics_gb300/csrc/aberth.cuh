@@ -386,6 +386,49 @@ __device__ bool aberth64_group(const cd (&p)[DEG + 1], cd &zr, int itmax, unsign
   return false;
 }
 
+// The FP32 Aberth stage on a group of G lanes, lane r < DEG iterating root r
+// from zr (every root updated from the previous iterate, roots exchanged by
+// shuffles), with the FP32 stopping rule of the reference's iteration; alpha =
+// |p_i| (1 + 3.8284271247461900976 i).  True when every root met the rule
+// within itcap iterations with finite values.
+template <int DEG, int G>
+__device__ bool aberth32_group(const cf (&ph)[DEG + 1], const float (&alpha)[DEG + 1], cf &zr, unsigned gmask,
+                               int itcap) {
+  const int r = threadIdx.x & (G - 1);
+  bool done = r >= DEG;
+  for (int it = 0; it < itcap; ++it) {
+    cf zall[DEG];
+#pragma unroll
+    for (int q = 0; q < DEG; ++q) zall[q] = mkf(__shfl_sync(gmask, zr.x, q, G), __shfl_sync(gmask, zr.y, q, G));
+    if (!done) {
+      const float az = cabs(zr);
+      const bool rev = az > 1.0f;
+      const cf x = rev ? crecip(zr) : zr;
+      cf h, hd;
+      float b;
+      horner_pair<DEG>(ph, alpha, x, rev ? 1.0f / az : az, rev, h, hd, b);
+      if (cabs(h) > CGB_EPS32 * b) {
+        cf sum = mkf(0.0f, 0.0f);
+#pragma unroll
+        for (int q = 0; q < DEG; ++q)
+          if (q != r) sum = sum + crecip(zr - zall[q]);
+        cf corr;
+        if (rev) {
+          const cf z2h = (zr * zr) * h, d = zr * h;
+          corr = cdiv(z2h, mkf(d.x * DEG, d.y * DEG) - hd - z2h * sum);
+        } else {
+          corr = cdiv(h, hd - h * sum);
+        }
+        zr = zr - corr;
+      } else {
+        done = true;
+      }
+    }
+    if (__all_sync(gmask, done)) return __all_sync(gmask, isfinite(zr.x) && isfinite(zr.y));
+  }
+  return false;
+}
+
 // FP64 Newton on one root of p (low -> high): at most SWEEPS steps, done when a
 // correction is at most 2^-40 |z|.  With sep2 = S^2 (default: infinite, the
 // plain rule only), S = sum_{k != j} 1/|z - z_k|

@@ -138,6 +138,9 @@ static int make_es_params(const cgb_lens_params &lens, double rho, const cgb_es_
   if (o->cta_threads != 0 && o->cta_threads != 64 && o->cta_threads != 128 && o->cta_threads != 256)
     return fail(CGB_ERR_INVALID, "cta_threads must be 0, 64, 128 or 256%s");
   P.threads = o->cta_threads;  // 0: chosen at launch (launch_es_variant)
+  if (o->point_lanes != 0 && o->point_lanes != 1 && o->point_lanes != 8)
+    return fail(CGB_ERR_INVALID, "point_lanes must be 0, 1 or 8%s");
+  P.point_lanes = o->point_lanes == 8 ? 8 : 1;
   if (o->labelling != 0 && o->labelling != 1) return fail(CGB_ERR_INVALID, "labelling must be 0 or 1%s");
   P.nearest = o->labelling;
   {

@@ -49,6 +49,7 @@ struct EsParams {
   int qchunk;                 // items taken per grab
   int ld_group;               // lanes sharing one contour point's quadrature nodes (1, 2, 4, 8)
   int threads;                // threads of a contour-kernel CTA (64, 128 or 256; 0 = chosen at launch)
+  int point_lanes;            // per-point pass: threads per polynomial (1, or 8 = a lane group per point)
   double grad_amp2;           // mixed adjoint: FP64 quadrature where max |dz/dtheta|^2 exceeds this
   int nearest;                // 1: nearest-root row labelling (no faithful solves)
   // row order of each item's first limb point, filled by es_first_order_kernel

@@ -116,6 +116,70 @@ __device__ __forceinline__ uint32_t images(const Lens &L, cd w, cd (&z)[NL * NL 
   return mask;
 }
 
+// images() on a group of G lanes (binary lenses): lane r < DEG iterates root
+// r of the point's polynomial, all roots updated together and exchanged by
+// shuffles, from FP32 initial estimates.  Mixed precision: the FP32 stage,
+// then an FP64 Newton polish of each lane's root and a distinctness check,
+// with the FP64 group iteration as the fallback; FP64: the FP64 group
+// iteration.  Every lane of the group calls it and gets all roots and the mask.
+template <int PREC, int G>
+__device__ uint32_t images_group(const Lens &L, cd w, cd (&z)[5], int itmax, uint32_t &flags, unsigned gmask) {
+  constexpr int DEG = 5;
+  const int r = threadIdx.x & (G - 1), gbase = (threadIdx.x & 31) - r;
+  cd p[DEG + 1];
+  lens_poly<2>(L, w, p);
+  cf ph[DEG + 1];
+  float alpha[DEG + 1];
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) {
+    ph[i] = tof(p[i]);
+    alpha[i] = cabs(ph[i]);
+  }
+  cf z0[DEG];
+  init_estimates_f32<DEG>(alpha, z0);
+  cf zf = z0[0];
+#pragma unroll
+  for (int q = 1; q < DEG; ++q)
+    if (q == r) zf = z0[q];
+  const cf zstart = zf;
+#pragma unroll
+  for (int i = 0; i <= DEG; ++i) alpha[i] *= fmaf(3.8284271247461900976f, (float)i, 1.0f);
+  cd zr;
+  bool ok;
+  if constexpr (PREC == MIXED) {
+    ok = aberth32_group<DEG, G>(ph, alpha, zf, gmask, min(itmax, 128));
+    zr = tod(zf);
+    const bool conv = r >= DEG || newton_polish_root<DEG, 5>(p, zr);
+    ok = __all_sync(gmask, ok && conv);
+    if (ok) {  // distinct roots (Newton alone may merge a near-double pair)
+      double scale = 0.0;
+      bool sep = true;
+#pragma unroll
+      for (int q = 0; q < DEG; ++q) {
+        const cd zq = mk(__shfl_sync(gmask, zr.x, q, G), __shfl_sync(gmask, zr.y, q, G));
+        scale = fmax(scale, norm2(zq));
+        if (r < DEG && q > r && norm2(zr - zq) < 1e-14 * fmax(norm2(zr), norm2(zq))) sep = false;
+      }
+      ok = __all_sync(gmask, sep);
+    }
+    if (!ok) {
+      flags |= CGB_ST_FALLBACK;
+      zr = tod(zstart);
+      ok = aberth64_group<DEG, G>(p, zr, itmax, gmask);
+    }
+  } else {
+    zr = tod(zstart);
+    ok = aberth64_group<DEG, G>(p, zr, itmax, gmask);
+  }
+  if (!ok) flags |= CGB_ST_NOCONV;
+#pragma unroll
+  for (int q = 0; q < DEG; ++q) z[q] = mk(__shfl_sync(gmask, zr.x, q, G), __shfl_sync(gmask, zr.y, q, G));
+  const double res = r < DEG ? cabs(lens_eq<2>(L, zr) - w) : 1.0;
+  const uint32_t mask = (__ballot_sync(gmask, r < DEG && res < 1e-6) >> gbase) & ((1u << DEG) - 1u);
+  if (__any_sync(gmask, r < DEG && res > 1e-6 / 30 && res < 1e-6 * 30)) flags |= CGB_ST_AMBIGUOUS;
+  return mask;
+}
+
 template <int PREC, int NL>
 __global__ void __launch_bounds__(PS_THREADS) mag_ps_kernel(Lens L, const cd *__restrict__ w, double *__restrict__ mag,
                                                             cd *__restrict__ images_out,
@@ -267,18 +331,24 @@ __device__ __forceinline__ int64_t curve_of(const int64_t *offsets, int64_t ncur
 // (forward-mode tangents through the images and the multipole series); the
 // contour kernel writes the rows of the queued points.  Curves with parameters
 // out of the domain give NaN, CGB_ST_INVALID and a zero row.
-template <int PREC, bool GRAD>
+// TPP: threads per polynomial (1, or a group of 8 lanes per point: forward
+// only); with a group, every lane evaluates the point and lane 0 writes it.
+template <int PREC, bool GRAD, int TPP>
 __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
     const CurveDev *__restrict__ curves, const int64_t *__restrict__ offsets, const double *__restrict__ times,
     int64_t ncurves, int64_t n, double *__restrict__ mag, uint8_t *__restrict__ route, uint32_t *__restrict__ status,
     int itmax, unsigned long long *qcount, int64_t *qlist, const double *__restrict__ cot, double *grow) {
-  const int64_t i = (int64_t)blockIdx.x * PS_THREADS + threadIdx.x;
-  if (i >= n) return;
+  static_assert(TPP == 1 || (TPP == 8 && !GRAD), "lane groups: forward only");
+  const int64_t i = ((int64_t)blockIdx.x * PS_THREADS + threadIdx.x) / TPP;
+  if (i >= n) return;  // whole groups: i is the same on every lane of a group
+  const int gr = threadIdx.x & (TPP - 1);
+  const bool writer = gr == 0;
   const int64_t c = curve_of(offsets, ncurves, i);
   const CurveDev cv = curves[c];
   if (!(cv.s > 0) || !(cv.q > 0) || !(cv.rho > 0) || !(cv.tE != 0) || !isfinite(cv.s) || !isfinite(cv.q) ||
       !isfinite(cv.rho) || !isfinite(cv.u1) || !isfinite(cv.u0) || !isfinite(cv.alpha) || !isfinite(cv.t0) ||
       !isfinite(cv.tE) || !isfinite(times[i])) {  // not evaluated: NaN, no gradient
+    if (!writer) return;
     mag[i] = __longlong_as_double(0x7ff8000000000000ll);
     route[i] = 0;
     if (status) status[i] = CGB_ST_INVALID;
@@ -297,6 +367,7 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
   // where the planetary test fails the point takes the contour integral whatever
   // its images give, so it is queued without them (the contour kernel writes mag)
   if (cv.q < 0.01 && !planetary_test(L, wi, cv.rho)) {
+    if (!writer) return;
     mag[i] = 0.0;
     route[i] = 1;
     if (status) status[i] = 0;
@@ -305,7 +376,13 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
   }
   uint32_t flags = 0;
   cd z[5];
-  uint32_t m = images<PREC, 2>(L, wi, z, itmax, flags);
+  uint32_t m;
+  if constexpr (TPP == 1) {
+    m = images<PREC, 2>(L, wi, z, itmax, flags);
+  } else {
+    const unsigned gmask = ((1u << TPP) - 1u) << ((threadIdx.x & 31) - gr);
+    m = images_group<PREC, TPP>(L, wi, z, itmax, flags, gmask);
+  }
   double mu_multi = 0.0, dmu = 0.0;
   cd W[5][5];
   double val[5];
@@ -322,6 +399,7 @@ __global__ void __launch_bounds__(PS_THREADS) lc_points_batched_kernel(
   }
   bool hex_ok = proximity_test_binary(L, wi, z, m, cv.rho, dmu);
   // (q < 0.01: the planetary test passed above)
+  if (!writer) return;
   mag[i] = mu_multi;
   route[i] = hex_ok ? 0 : 1;
   if (status) status[i] = flags;
@@ -378,15 +456,22 @@ template <int PREC>
 cudaError_t launch_lc_points_batched_p(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
                                        unsigned long long *qcount, int64_t *qlist, bool grad, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
-  if (grad)
-    lc_points_batched_kernel<PREC, true><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n,
-                                                                          mag, route, status, P.itmax, qcount, qlist,
-                                                                          P.cot, P.grow);
-  else
-    lc_points_batched_kernel<PREC, false><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n,
-                                                                           mag, route, status, P.itmax, qcount, qlist,
-                                                                           nullptr, nullptr);
+  if (grad) {
+    dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+    lc_points_batched_kernel<PREC, true, 1><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves, n,
+                                                                             mag, route, status, P.itmax, qcount,
+                                                                             qlist, P.cot, P.grow);
+  } else if (P.point_lanes == 8) {
+    dim3 grid((unsigned)((n * 8 + PS_THREADS - 1) / PS_THREADS));
+    lc_points_batched_kernel<PREC, false, 8><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves,
+                                                                              n, mag, route, status, P.itmax, qcount,
+                                                                              qlist, nullptr, nullptr);
+  } else {
+    dim3 grid((unsigned)((n + PS_THREADS - 1) / PS_THREADS));
+    lc_points_batched_kernel<PREC, false, 1><<<grid, PS_THREADS, 0, stream>>>(P.curves, P.offsets, P.times, P.ncurves,
+                                                                              n, mag, route, status, P.itmax, qcount,
+                                                                              qlist, nullptr, nullptr);
+  }
   return cudaGetLastError();
 }
 

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define CGB_ABI_VERSION 3
+#define CGB_ABI_VERSION 4
 
 /* launch status */
 #define CGB_OK 0
@@ -86,6 +86,11 @@ typedef struct cgb_es_options {
                              else 256); fewer threads let more evaluations share an SM where shared
                              memory allows (the phases run on few threads at small npts_limb); a
                              launch-shape knob that changes results only in the summation order */
+  int32_t point_lanes;    /* batched light curves, per-point pass (roots, hexadecapole, routing): threads per
+                             polynomial, 0 or 1 = one thread per point, 8 = a group of 8 lanes per point
+                             (one lane per root, simultaneous Aberth steps; forward only, the adjoint's
+                             pass takes one thread per point); roots agree to rounding, so results and
+                             routing agree except where a point's test sits on its threshold */
 } cgb_es_options;
 
 /* Parameters of one binary-lens light curve for the batched entry points: lens

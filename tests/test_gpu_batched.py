@@ -17,6 +17,7 @@ from oracle import caustics_oracle as O
 
 pytestmark = pytest.mark.gpu
 C = pytest.importorskip("caustics_gb300")
+from caustics_gb300 import _lib as L  # noqa: E402
 
 
 def draw_curves(ncurves, seed, nmin=20, nmax=60):
@@ -146,7 +147,7 @@ def test_autotuned_graph_evaluator():
     off, t, cv = draw_curves(6, seed=11)
     ev = C.BatchedLightCurves(off, t, curves_for_tuning=cv, precision="mixed", **OPTS)
     assert ev.graph is not None, ev.graph_error
-    assert set(ev.config) == {"grid", "queue_chunk", "ld_group", "cta_threads"}
+    assert set(ev.config) == {"grid", "queue_chunk", "ld_group", "cta_threads", "point_lanes"}
     for seed in (11, 12):
         _, _, cv2 = draw_curves(6, seed=seed)
         m = ev(torch.as_tensor(cv2, device="cuda")).cpu().numpy()
@@ -158,7 +159,8 @@ def test_autotuned_graph_evaluator():
 
 @pytest.mark.parametrize("cfg", [dict(grid=7, queue_chunk=3, ld_group=4), dict(grid=1, queue_chunk=1, ld_group=8),
                                  dict(grid=0, queue_chunk=2, ld_group=2), dict(grid=0, cta_threads=128),
-                                 dict(grid=5, cta_threads=64, ld_group=2)])
+                                 dict(grid=5, cta_threads=64, ld_group=2), dict(point_lanes=8),
+                                 dict(grid=0, cta_threads=128, point_lanes=8)])
 def test_launch_shapes_agree(cfg):
     """Every launch shape the autotuner can pick gives the same magnifications."""
     off, t, cv = draw_curves(5, seed=13)
@@ -168,3 +170,27 @@ def test_launch_shapes_agree(cfg):
     g0, _ = C.mag_lc_batched_vjp(off, t, cv, np.ones(len(t)), precision="fp64", **OPTS)
     g1, _ = C.mag_lc_batched_vjp(off, t, cv, np.ones(len(t)), precision="fp64", **cfg, **OPTS)
     assert torch.allclose(g0, g1, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_point_lanes_group_solver(precision):
+    """The per-point pass with a group of 8 lanes per polynomial (one lane per
+    root) against one thread per polynomial: the same routing, hexadecapole
+    magnifications equal to rounding, over curves whose points take both
+    routes; the flags of the group solve are the thread solve's bits."""
+    off, t, cv = draw_curves(12, seed=21)
+    m1, r1, s1 = C.mag_lc_batched(off, t, cv, precision=precision, return_route=True, return_status=True, **OPTS)
+    m8, r8, s8 = C.mag_lc_batched(off, t, cv, precision=precision, return_route=True, return_status=True,
+                                  point_lanes=8, **OPTS)
+    assert torch.equal(r1, r8)
+    assert (~r1).sum().item() > 0 and r1.sum().item() > 0
+    hex_ = ~r1
+    assert torch.allclose(m8[hex_], m1[hex_], rtol=1e-11, atol=0)
+    assert torch.allclose(m8[r1], m1[r1], rtol=1e-12, atol=0)
+    assert not ((s8 | s1) & (L.ST_INVALID | L.ST_CAPACITY)).any()
+
+
+def test_point_lanes_refused_values():
+    off, t, cv = draw_curves(2, seed=3)
+    with pytest.raises(L.CausticsError, match="point_lanes"):
+        C.mag_lc_batched(off, t, cv, precision="fp64", point_lanes=4, **OPTS)
