@@ -68,17 +68,17 @@ def f_es(L, G):
 # FP32 arithmetic (dadd + dmul + 2 dfma, fadd + fmul + 2 ffma thread
 # instructions).
 NCU_EVALS = 2764
-DRAM_BYTES_PER_EVAL = 5.601e6 / NCU_EVALS
-FP64_FLOP_PER_EVAL = 1.1711e9 / NCU_EVALS
-FP32_FLOP_PER_EVAL = 2.3639e10 / NCU_EVALS
-FP64_PIPE_BUSY_NCU = 0.573
+DRAM_BYTES_PER_EVAL = 5.667e6 / NCU_EVALS
+FP64_FLOP_PER_EVAL = 1.1378e9 / NCU_EVALS
+FP32_FLOP_PER_EVAL = 2.3732e10 / NCU_EVALS
+FP64_PIPE_BUSY_NCU = 0.571
 # the same for es_kernel<2, MIXED, GRAD> (the VJP's contour kernel), one
 # launch over 2000 contour evaluations of the gradient workload
 NCU_EVALS_VJP = 2000
-DRAM_BYTES_PER_EVAL_VJP = 55.24e6 / NCU_EVALS_VJP
-FP64_FLOP_PER_EVAL_VJP = 4.4575e9 / NCU_EVALS_VJP
-FP32_FLOP_PER_EVAL_VJP = 6.3113e10 / NCU_EVALS_VJP
-FP64_PIPE_BUSY_NCU_VJP = 0.706
+DRAM_BYTES_PER_EVAL_VJP = 51.58e6 / NCU_EVALS_VJP
+FP64_FLOP_PER_EVAL_VJP = 4.3083e9 / NCU_EVALS_VJP
+FP32_FLOP_PER_EVAL_VJP = 6.3180e10 / NCU_EVALS_VJP
+FP64_PIPE_BUSY_NCU_VJP = 0.693
 
 
 def draw_batched(ncurves_total, seed, nmin, nmax, take):
