@@ -961,9 +961,12 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
     const double a = isQ ? z0.x : z0.y, b = isQ ? zc.x : zc.y;
     double sp, dsa, dsb, dsr;
     split_point_grad(a, b, rho, sp, dsa, dsb, dsr);
-    double val = 0.0, fixed = 0.0, kk[NK], dlo[2], dhi[2];
+    // the two halves' sums: FP64 for the FP64 quadrature, FP32 for FP32 nodes
+    // (the halves cancel by at most a factor 2: the reference's split point
+    // a + |b - a| / 2 can lie beyond a when b < a)
+    R val = 0, fixed = 0, kk[NK], dlo[2], dhi[2];
 #pragma unroll
-    for (int k = 0; k < NK; ++k) kk[k] = 0.0;
+    for (int k = 0; k < NK; ++k) kk[k] = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const double lo = half ? sp : a, hi = half ? b : sp;
@@ -1047,31 +1050,32 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
 #pragma unroll
         for (int m = 0; m < NLD; ++m) Ck[GK_A + m] += w * dIdr * ((sh.x * dsl[m].x + sh.y * dsl[m].y) * irho);
       }
-      val += (double)hw * (double)A;
-      fixed += (double)hw * (double)Cf;
+      val += hw * A;
+      fixed += hw * Cf;
 #pragma unroll
-      for (int k = 0; k < NK; ++k) kk[k] += (double)hw * (double)Ck[k];
-      dlo[half] = -0.5 * (double)A + (double)hw * (double)Bl;
-      dhi[half] = 0.5 * (double)A + (double)hw * (double)Bh;
+      for (int k = 0; k < NK; ++k) kk[k] += hw * Ck[k];
+      dlo[half] = (R)-0.5 * A + hw * Bl;
+      dhi[half] = (R)0.5 * A + hw * Bh;
     }
-    const double dsp = dhi[0] + dlo[1];
-    const double d_a = dlo[0] + dsp * dsa, d_b = dhi[1] + dsp * dsb;
-    kk[GK_RHO] += dsp * dsr;
+    const double dsp = (double)dhi[0] + (double)dlo[1];
+    const double d_a = (double)dlo[0] + dsp * dsa, d_b = (double)dhi[1] + dsp * dsb;
     const double f = isQ ? 0.5 : -0.5;
     if (!isQ) {
-      g.P = f * val;
+      g.P = f * (double)val;
       g.Py = f * d_b;
       g.Pa = f * d_a;
-      g.Px = f * fixed;
+      g.Px = f * (double)fixed;
 #pragma unroll
-      for (int k = 0; k < NK; ++k) g.Pk[k] = f * kk[k];
+      for (int k = 0; k < NK; ++k) g.Pk[k] = f * (double)kk[k];
+      g.Pk[GK_RHO] += f * dsp * dsr;
     } else {
-      g.Q = f * val;
+      g.Q = f * (double)val;
       g.Qx = f * d_b;
       g.Qa = f * d_a;
-      g.Qy = f * fixed;
+      g.Qy = f * (double)fixed;
 #pragma unroll
-      for (int k = 0; k < NK; ++k) g.Qk[k] = f * kk[k];
+      for (int k = 0; k < NK; ++k) g.Qk[k] = f * (double)kk[k];
+      g.Qk[GK_RHO] += f * dsp * dsr;
     }
   }
 }
