@@ -938,18 +938,22 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
   constexpr int NK = GradDirs<NL>::NK, NLD = GradDirs<NL>::NLENS;
   // shifted lens equation around the contour point
   const double rho = It.rho, inv_rho = 1.0 / rho;
-  const cd uc64 = (lens_eq<NL>(It.L, zc) - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
-  C uc = C{(R)uc64.x, (R)uc64.y};
+  // D_j = conj(zc) - conj(r_j) and 1 / D_j, which lens_eq(zc) = zc - sum_j
+  // eps_j / D_j uses too (the same operations in the same order as lens_eq)
   C Dj[NL], iDj[NL];
   R ej[NL];
+  cd lez = zc;
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
     cd d = conj(zc) - conj(It.L.r[k]);
     cd id = crecip(d);
+    lez = lez - id * It.L.eps[k];
     Dj[k] = C{(R)d.x, (R)d.y};
     iDj[k] = C{(R)id.x, (R)id.y};
     ej[k] = (R)It.L.eps[k];
   }
+  const cd uc64 = (lez - It.w0) * inv_rho;  // (lens_eq(zc) - w0) / rho
+  C uc = C{(R)uc64.x, (R)uc64.y};
   const R irho = (R)inv_rho, u1 = (R)It.u1;
   const R c0 = (R)(3.0 / (3.0 - It.u1)), dc0 = (R)(3.0 / ((3.0 - It.u1) * (3.0 - It.u1)));
   // 1 - |s/rho|^2 = (1 - |uc|^2) - 2 Re(conj(uc) dl) - |dl|^2 with the first
