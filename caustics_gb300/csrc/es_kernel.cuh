@@ -29,8 +29,11 @@
 //     nodes;
 //  and with GRAD the hand-written adjoint of A-F (contours recomputed).
 #pragma once
+#include <type_traits>
+
 #include "aberth.cuh"
 #include "aberth_ref.cuh"
+#include "dword.cuh"
 #include "es.h"
 #include "internal.h"
 
@@ -755,7 +758,7 @@ __device__ __forceinline__ LdConst ld_const(const EsItem &It) {
 // ones the node loop would otherwise do per node).
 template <int NL>
 __device__ cd ld_point_mixed(const EsParams &P, const EsItem &It, const LdConst &K, cd zc, double th, cd z0, int j0,
-                             int jstep, const float (*glf)[2][GL_MAX]) {
+                             int jstep, const float (*glf)[4][GL_MAX]) {
   // I = c0 (u1 B + 1 - 2 u1) = cu B + cc
   const float cu = K.c0 * K.u1, cc = K.c0 * (1.0f - 2.0f * K.u1);
   cf uc;
@@ -934,7 +937,7 @@ constexpr float X1_COND = 1e2f * 8.0f * 5.9604645e-8f;
 
 template <int NL, typename R, typename C>
 __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad<GradDirs<NL>::NK> &g,
-                           const float (*glf)[2][GL_MAX]) {
+                           const float (*glf)[4][GL_MAX]) {
   constexpr int NK = GradDirs<NL>::NK, NLD = GradDirs<NL>::NLENS;
   // shifted lens equation around the contour point
   const double rho = It.rho, inv_rho = 1.0 / rho;
@@ -982,9 +985,12 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
       for (int k = 0; k < NK; ++k) Ck[k] = 0;
       for (int j = 0; j < n; ++j) {
         R t, w;
-        if constexpr (sizeof(R) == sizeof(float)) {
+        if constexpr (std::is_same<R, float>::value) {
           t = glf[half][0][j];
           w = glf[half][1][j];
+        } else if constexpr (std::is_same<R, dw>::value) {
+          t = dw(glf[half][0][j], glf[half][2][j]);
+          w = dw(glf[half][1][j], glf[half][3][j]);
         } else {
           t = P.gl_x[half][j];
           w = P.gl_w[half][j];
@@ -1001,7 +1007,7 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         }
         const C srho = C{uc.x + dl.x, uc.y + dl.y};
         R x1 = c1 - (R)2 * (uc.x * dl.x + uc.y * dl.y) - (dl.x * dl.x + dl.y * dl.y);  // 1 - r^2
-        if constexpr (sizeof(R) == sizeof(float)) {
+        if constexpr (std::is_same<R, float>::value) {
           const float dln = fabsf(dl.x) + fabsf(dl.y);
           if (fabsf(x1) < X1_COND * dln * (1.0f + dln)) {
             NodeLens<NL> nl;
@@ -1128,7 +1134,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
                             const int *cstart, const int *cpar, const cd *centroid,
                             double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2],
                             double (*cgr_w)[MAX_CLOSED + N_CONTOURS][2], double (*pgr_w)[NK_MAX], double *tot_sh,
-                            int64_t pi, double *mag, const float (*glf)[2][GL_MAX]) {
+                            int64_t pi, double *mag, const float (*glf)[4][GL_MAX]) {
   constexpr int DEG = NL * NL + 1, NK = GradDirs<NL>::NK;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
@@ -1184,7 +1190,8 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
           if (PREC == MIXED && amp2 <= P.grad_amp2)
             ld_pq_grad<NL, float, cf>(P, I, zc, centroid[c], g, glf);
           else
-            ld_pq_grad<NL, double, cd>(P, I, zc, centroid[c], g, glf);
+            ld_pq_grad<NL, typename std::conditional<PREC == MIXED, dw, double>::type,
+                       typename std::conditional<PREC == MIXED, cdw, cd>::type>(P, I, zc, centroid[c], g, glf);
           const cd pq = mk(g.P, g.Q);
           atomicAdd(&S.GG[i].x, pc * (wx * g.Px + wy * g.Qx));
           atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
@@ -1434,11 +1441,16 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
   __shared__ double cgr_w[GRAD ? ES_MAX_WARPS : 1][MAX_CLOSED + N_CONTOURS][2];
   __shared__ double pgr_w[GRAD ? ES_MAX_WARPS : 1][NK_MAX];
   __shared__ double tot_sh;
-  __shared__ float glf[2][2][GL_MAX];  // FP32 Gauss-Legendre tables [half][nodes | weights][j]
+  // FP32 Gauss-Legendre tables [half][nodes | weights | their low words][j]:
+  // the FP32 nodes use the first two, the adjoint's double-word quadrature all four
+  __shared__ float glf[2][4][GL_MAX];
   for (int i = threadIdx.x; i < 2 * GL_MAX; i += ES_THREADS) {
     const int h = i / GL_MAX, j = i % GL_MAX;
-    glf[h][0][j] = (float)P.gl_x[h][j];
-    glf[h][1][j] = (float)P.gl_w[h][j];
+    const dw x(P.gl_x[h][j]), w(P.gl_w[h][j]);
+    glf[h][0][j] = x.hi;
+    glf[h][1][j] = w.hi;
+    glf[h][2][j] = x.lo;
+    glf[h][3][j] = w.lo;
   }
   const int Lcap = P.Lcap;
   EsSmem<DEG> S;
