@@ -75,10 +75,10 @@ FP64_PIPE_BUSY_NCU = 0.571
 # the same for es_kernel<2, MIXED, GRAD> (the VJP's contour kernel), one
 # launch over 2000 contour evaluations of the gradient workload
 NCU_EVALS_VJP = 2000
-DRAM_BYTES_PER_EVAL_VJP = 51.58e6 / NCU_EVALS_VJP
-FP64_FLOP_PER_EVAL_VJP = 4.3083e9 / NCU_EVALS_VJP
-FP32_FLOP_PER_EVAL_VJP = 6.3180e10 / NCU_EVALS_VJP
-FP64_PIPE_BUSY_NCU_VJP = 0.693
+DRAM_BYTES_PER_EVAL_VJP = 28.79e6 / NCU_EVALS_VJP
+FP64_FLOP_PER_EVAL_VJP = 3.3826e9 / NCU_EVALS_VJP
+FP32_FLOP_PER_EVAL_VJP = 7.1830e10 / NCU_EVALS_VJP
+FP64_PIPE_BUSY_NCU_VJP = 0.620
 
 
 def draw_batched(ncurves_total, seed, nmin, nmax, take):
