@@ -368,14 +368,18 @@ def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, n
 # ---------------------------------------------------------------------------
 
 CURVE_FIELDS = ("s", "q", "rho", "u1", "u0", "alpha", "t0", "tE")
+CURVE_FIELDS_TRIPLE = ("s", "q", "q3", "r3", "psi", "rho", "u1", "u0", "alpha", "t0", "tE")
 
 
-def _batched_args(offsets, t, curves):
+def _batched_args(offsets, t, curves, triple=False):
     off, _ = _to_device(offsets, torch.int64)
     tt, _ = _to_device(t, torch.float64)
     cv, _ = _to_device(curves, torch.float64)
-    if cv.ndim != 2 or cv.shape[1] != 8:
-        raise ValueError("curves must have shape [ncurves, 8]: " + ", ".join(CURVE_FIELDS))
+    if not triple and (cv.ndim != 2 or cv.shape[1] != 8):
+        raise ValueError("curves must have shape [ncurves, 8]: " + ", ".join(CURVE_FIELDS) +
+                         " (triple lenses: [ncurves, 11]: " + ", ".join(CURVE_FIELDS_TRIPLE) + ")")
+    if triple and (cv.ndim != 2 or cv.shape[1] != 11):
+        raise ValueError("triple-lens curves must have shape [ncurves, 11]: " + ", ".join(CURVE_FIELDS_TRIPLE))
     if off.numel() != cv.shape[0] + 1:
         raise ValueError("offsets must have ncurves + 1 entries")
     return off.contiguous(), tt.contiguous(), cv.contiguous()
@@ -389,14 +393,18 @@ def _workspace(n, device, vjp=False):
 
 def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
                    precision="mixed", grid=0, queue_chunk=1, ld_group=1, return_route=False, return_status=False,
-                   out=None, labelling="reference", cta_threads=0, point_lanes=0):
-    """mag() for many binary-lens light curves of uneven lengths in one pass.
+                   out=None, labelling="reference", cta_threads=0, point_lanes=0, triple_routing="contour"):
+    """mag() for many light curves of uneven lengths in one pass.
 
     offsets: int64 [ncurves+1]; t: float64 [npoints]; curves: float64
-    [ncurves, 8] = (s, q, rho, u1, u0, alpha, t0, tE) per curve, the source on
-    the rectilinear trajectory.  Per-curve u1 is used when limb_darkening.
-    grid, queue_chunk, ld_group, cta_threads, point_lanes: launch shape (autotune.tune)."""
-    off, tt, cv = _batched_args(offsets, t, curves)
+    [ncurves, 8] = (s, q, rho, u1, u0, alpha, t0, tE) per binary-lens curve, or
+    [ncurves, 11] = (s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE) per
+    triple-lens curve (every point through the contour integral, as the
+    reference's mag()); the source on the rectilinear trajectory.  Per-curve u1
+    is used when limb_darkening.  grid, queue_chunk, ld_group, cta_threads,
+    point_lanes: launch shape (autotune.tune)."""
+    triple = np.ndim(curves) == 2 and np.shape(curves)[1] == 11
+    off, tt, cv = _batched_args(offsets, t, curves, triple)
     n = tt.numel()
     dev = tt.device
     if out is None:
@@ -408,10 +416,12 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
         mag_out, route, st, ws = out
         nbytes = ws.numel()
     opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
-                       labelling=labelling, cta_threads=cta_threads, point_lanes=point_lanes)
+                       labelling=labelling, cta_threads=cta_threads, point_lanes=point_lanes,
+                       triple_routing=triple_routing)
+    fn = "cgb_mag_lc_batched_triple" if triple else "cgb_mag_lc_batched"
     with torch.cuda.device(dev):
-        L.check(L.lib().cgb_mag_lc_batched(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
-                                           _ptr(st), opts, _ptr(ws), nbytes, _stream()), "cgb_mag_lc_batched")
+        L.check(getattr(L.lib(), fn)(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(mag_out), _ptr(route),
+                                     _ptr(st), opts, _ptr(ws), nbytes, _stream()), fn)
     res = [mag_out]
     if return_route:
         res.append(route.bool())

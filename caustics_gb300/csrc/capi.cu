@@ -353,16 +353,23 @@ size_t cgb_mag_lc_batched_vjp_workspace_bytes(int64_t npoints) {
   return cgb_mag_lc_batched_workspace_bytes(npoints) + 64 * (size_t)(npoints > 0 ? npoints : 0);
 }
 
-static int batched_setup(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
-                         int64_t npoints, const cgb_es_options *opts, void *ws, size_t ws_bytes, EsParams &P) {
+// nl: 2 (curves: cgb_curve_params) or 3 (cgb_curve_params_triple); the
+// options are checked against a lens of that many masses (shared memory).
+static int batched_setup(const int64_t *offsets, const double *t, const void *curves, int64_t ncurves,
+                         int64_t npoints, const cgb_es_options *opts, void *ws, size_t ws_bytes, EsParams &P,
+                         int nl = 2) {
   if (ncurves < 1 || npoints < 0) return fail(CGB_ERR_INVALID, "need ncurves >= 1 and npoints >= 0%s");
   if (!offsets || !curves || (npoints > 0 && !t)) return fail(CGB_ERR_INVALID, "null buffer%s");
   if (!ws || ws_bytes < batched_queue_bytes(npoints))
     return fail(CGB_ERR_INVALID, "workspace too small (see cgb_mag_lc_batched_workspace_bytes)%s");
-  cgb_lens_params dummy{2, 1.0, 1.0, 0.0, 0.0, 0.0};
+  const cgb_lens_params dummy = nl == 3 ? cgb_lens_params{3, 1.0, 0.5, 0.1, 1.0, 0.0}
+                                        : cgb_lens_params{2, 1.0, 1.0, 0.0, 0.0, 0.0};
   int rc = make_es_params(dummy, 1.0, opts, P);
   if (rc) return rc;
-  P.curves = reinterpret_cast<const CurveDev *>(curves);
+  if (nl == 3)
+    P.curves3 = reinterpret_cast<const CurveDev3 *>(curves);
+  else
+    P.curves = reinterpret_cast<const CurveDev *>(curves);
   P.offsets = offsets;
   P.times = t;
   P.ncurves = ncurves;
@@ -394,6 +401,27 @@ int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_
   if (rc) return rc;
   return cuda_status(launch_es_routed(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
                      "cgb_mag_lc_batched contour pass");
+}
+
+int cgb_mag_lc_batched_triple(const int64_t *offsets, const double *t, const cgb_curve_params_triple *curves,
+                              int64_t ncurves, int64_t npoints, double *mag, uint8_t *route, uint32_t *status,
+                              const cgb_es_options *opts, void *workspace, size_t workspace_bytes, void *stream) {
+  if (npoints > 0 && (!mag || !route)) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (opts && opts->triple_routing != 0)
+    return fail(CGB_ERR_UNSUPPORTED, "batched triple-lens light curves take triple_routing 0%s");
+  EsParams P;
+  int rc = batched_setup(offsets, t, curves, ncurves, npoints, opts, workspace, workspace_bytes, P, 3);
+  if (rc) return rc;
+  if (npoints == 0) return CGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = cuda_status(cudaMemsetAsync(workspace, 0, 16, s), "queue reset");
+  if (rc) return rc;
+  rc = cuda_status(launch_lc_points_batched_triple(P, npoints, mag, route, status, (unsigned long long *)workspace,
+                                                   (int64_t *)((char *)workspace + 16), s),
+                   "cgb_mag_lc_batched_triple point pass");
+  if (rc) return rc;
+  return cuda_status(launch_es_routed(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
+                     "cgb_mag_lc_batched_triple contour pass");
 }
 
 int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,

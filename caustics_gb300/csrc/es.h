@@ -13,6 +13,11 @@ constexpr int GL_MAX = 64;  // Gauss-Legendre nodes per half interval
 struct CurveDev {
   double s, q, rho, u1, u0, alpha, t0, tE;
 };
+// a triple-lens light curve: the lens as cgb_lens_params (s, q, q3, r3, psi),
+// then the source and trajectory as CurveDev
+struct CurveDev3 {
+  double s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE;
+};
 
 // The lens / source of the item a CTA is integrating.
 struct EsItem {
@@ -39,6 +44,7 @@ struct EsParams {
   // c with offsets[c] <= i < offsets[c+1]; its source is on the rectilinear
   // trajectory at times[i] (trajectory.py:152-155 with pi_E = 0)
   const CurveDev *curves;
+  const CurveDev3 *curves3;  // triple-lens light curves (forward only), instead of curves
   const int64_t *offsets;
   const double *times;
   int64_t ncurves;
@@ -93,6 +99,9 @@ cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t 
 // Per-point pass of batched light curves; routed points are appended to the
 // device queue (qcount, qlist).  grad: hexadecapole-routed points add their
 // cotangent-weighted gradient to P.cgrad.
+cudaError_t launch_lc_points_batched_triple(const EsParams &P, int64_t n, double *mag, uint8_t *route,
+                                            uint32_t *status, unsigned long long *qcount, int64_t *qlist,
+                                            cudaStream_t stream);
 cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
                                      int precision, unsigned long long *qcount, int64_t *qlist, bool grad,
                                      cudaStream_t stream);

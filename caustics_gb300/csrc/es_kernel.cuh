@@ -1331,7 +1331,25 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
 // source centre of a single lens.
 __device__ __forceinline__ EsItem make_item(const EsParams &P, const cd *w0s, int64_t pi) {
   EsItem it;
-  if (P.curves) {
+  if (P.curves3) {  // triple-lens light curves
+    int64_t lo = 0, hi = P.ncurves - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (P.offsets[mid] <= pi) lo = mid; else hi = mid - 1;
+    }
+    const CurveDev3 cv = P.curves3[lo];
+    it.L = make_lens(3, cv.s, cv.q, cv.q3, cv.r3, cv.psi);
+    it.rho = cv.rho;
+    it.u1 = P.ld ? cv.u1 : 0.0;
+    const double tau = (P.times[pi] - cv.t0) / cv.tE;
+    double sa, ca;
+    sincos(cv.alpha, &sa, &ca);
+    it.w0 = mk(cv.u0 * ca + tau * sa + it.L.x_cm, -cv.u0 * sa + tau * ca);
+    it.s = cv.s;
+    it.q = cv.q;
+    it.curve = lo;
+    it.tau = tau;
+  } else if (P.curves) {
     int64_t lo = 0, hi = P.ncurves - 1;
     while (lo < hi) {
       const int64_t mid = (lo + hi + 1) >> 1;

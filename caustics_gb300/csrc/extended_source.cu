@@ -39,7 +39,7 @@ static cudaError_t dispatch_es(const EsParams &P, const double *w0, const int64_
                                cudaStream_t stream) {
   if (n == 0 && !P.qhead) return cudaSuccess;
   const cd *w = reinterpret_cast<const cd *>(w0);
-  const int nl = P.curves ? 2 : P.L.n;
+  const int nl = P.curves3 ? 3 : (P.curves ? 2 : P.L.n);
   if (nl == 2)
     return precision == MIXED ? launch_es_variant<2, MIXED, false>(P, w, index, route, n, mag, status, grid, stream)
                               : launch_es_variant<2, FP64, false>(P, w, index, route, n, mag, status, grid, stream);

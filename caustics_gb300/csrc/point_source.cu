@@ -3,6 +3,7 @@
 // runtime precision.  The light-curve point passes only take FP64 or MIXED.
 // Also two precision-free kernels: the lens-equation polynomial of source
 // positions, and the per-curve sums of the batched adjoint's point rows.
+#include "aberth.cuh"
 #include "es.h"
 #include "internal.h"
 
@@ -22,6 +23,47 @@ cudaError_t launch_lc_points_batched_p(const EsParams &P, int64_t n, double *mag
                                        unsigned long long *qcount, int64_t *qlist, bool grad, cudaStream_t stream);
 
 constexpr int AUX_THREADS = 128;
+
+// The per-point pass of triple-lens light curves: the reference's mag() sends
+// every triple-lens point to the contour integral (src/caustics/lightcurve.py:
+// 226-227), so a point is checked and queued; the contour kernel writes mag.
+__global__ void __launch_bounds__(AUX_THREADS)
+    lc_points_batched_triple_kernel(const CurveDev3 *__restrict__ curves, const int64_t *__restrict__ offsets,
+                                    const double *__restrict__ times, int64_t ncurves, int64_t n,
+                                    double *__restrict__ mag, uint8_t *__restrict__ route,
+                                    uint32_t *__restrict__ status, unsigned long long *qcount, int64_t *qlist) {
+  const int64_t i = (int64_t)blockIdx.x * AUX_THREADS + threadIdx.x;
+  if (i >= n) return;
+  int64_t lo = 0, hi = ncurves - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= i) lo = mid; else hi = mid - 1;
+  }
+  const CurveDev3 cv = curves[lo];
+  const bool ok = cv.s > 0 && cv.q > 0 && cv.q3 >= 0 && cv.rho > 0 && cv.tE != 0 && isfinite(cv.s) &&
+                  isfinite(cv.q) && isfinite(cv.q3) && isfinite(cv.r3) && isfinite(cv.psi) && isfinite(cv.rho) &&
+                  isfinite(cv.u1) && isfinite(cv.u0) && isfinite(cv.alpha) && isfinite(cv.t0) && isfinite(cv.tE) &&
+                  isfinite(times[i]);
+  if (!ok) {  // not evaluated: NaN
+    mag[i] = __longlong_as_double(0x7ff8000000000000ll);
+    route[i] = 0;
+    if (status) status[i] = CGB_ST_INVALID;
+    return;
+  }
+  mag[i] = 0.0;
+  route[i] = 1;
+  if (status) status[i] = 0;
+  qlist[atomicAdd(qcount, 1ull)] = i;
+}
+
+cudaError_t launch_lc_points_batched_triple(const EsParams &P, int64_t n, double *mag, uint8_t *route,
+                                            uint32_t *status, unsigned long long *qcount, int64_t *qlist,
+                                            cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  lc_points_batched_triple_kernel<<<(unsigned)((n + AUX_THREADS - 1) / AUX_THREADS), AUX_THREADS, 0, stream>>>(
+      P.curves3, P.offsets, P.times, P.ncurves, n, mag, route, status, qcount, qlist);
+  return cudaGetLastError();
+}
 
 // cgrad[c][k] = sum of the rows grow[i][k] of curve c's points: one warp per
 // curve, each lane summing a fixed stride of points, then a fixed shuffle tree,

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define CGB_ABI_VERSION 4
+#define CGB_ABI_VERSION 5
 
 /* launch status */
 #define CGB_OK 0
@@ -101,6 +101,14 @@ typedef struct cgb_es_options {
 typedef struct cgb_curve_params {
   double s, q, rho, u1, u0, alpha, t0, tE;
 } cgb_curve_params;
+
+/* One triple-lens light curve: the lens as cgb_lens_params (s, q, q3, r3, psi;
+ * masses e1 = q/(1+q+q3), e2 = q e1, third lens at r3 e^{i psi},
+ * src/caustics/point_source.py:1807-1817), then the source and the
+ * trajectory as cgb_curve_params. */
+typedef struct cgb_curve_params_triple {
+  double s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE;
+} cgb_curve_params_triple;
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *cgb_last_error(void);
@@ -236,6 +244,19 @@ size_t cgb_mag_lc_batched_workspace_bytes(int64_t npoints);
 int cgb_mag_lc_batched(const int64_t *offsets, const double *t, const cgb_curve_params *curves, int64_t ncurves,
                        int64_t npoints, double *mag, uint8_t *route, uint32_t *status, const cgb_es_options *opts,
                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* cgb_mag_lc_batched for triple-lens light curves (curves:
+ * cgb_curve_params_triple[ncurves], device), forward only: as the reference's
+ * mag() (src/caustics/lightcurve.py:226-227) every point takes the contour
+ * integral (route 1), so opts->triple_routing must be 0 (else
+ * CGB_ERR_UNSUPPORTED).  Same workspace as cgb_mag_lc_batched.  Under
+ * CGB_PREC_MIXED a curve with a mass fraction below 1e-2 keeps the mixed
+ * solver (its roots fall back to FP64 one by one: correct, slower); the
+ * single-curve cgb_mag takes FP64 for such lenses from the start, and
+ * precision FP64 does the same here. */
+int cgb_mag_lc_batched_triple(const int64_t *offsets, const double *t, const cgb_curve_params_triple *curves,
+                              int64_t ncurves, int64_t npoints, double *mag, uint8_t *route, uint32_t *status,
+                              const cgb_es_options *opts, void *workspace, size_t workspace_bytes, void *stream);
 
 /* cgb_mag_lc_batched without a workspace argument and without allocating: the
  * queue (and, for calls of at most 131,072 points, the first-limb-point row

@@ -194,3 +194,65 @@ def test_point_lanes_refused_values():
     off, t, cv = draw_curves(2, seed=3)
     with pytest.raises(L.CausticsError, match="point_lanes"):
         C.mag_lc_batched(off, t, cv, precision="fp64", point_lanes=4, **OPTS)
+
+
+def draw_triple_curves(ncurves, seed, nmin=10, nmax=20):
+    """Triple-lens curves: lenses drawn as the triple point-source workload (s,
+    r3 ~ U[0.5, 2], q ~ logU[1e-4, 1], q3 ~ logU[1e-4, 1e-1], psi ~ U[0, 2pi]),
+    sources and trajectories as the batched workload."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(nmin, nmax + 1, ncurves)
+    cv = np.stack([rng.uniform(0.5, 2, ncurves), 10 ** rng.uniform(-4, 0, ncurves), 10 ** rng.uniform(-4, -1, ncurves),
+                   rng.uniform(0.5, 2, ncurves), rng.uniform(0, 2 * np.pi, ncurves),
+                   10 ** rng.uniform(-3, -1.5, ncurves), rng.uniform(0.2, 0.8, ncurves), rng.uniform(-0.3, 0.3, ncurves),
+                   rng.uniform(0, 2 * np.pi, ncurves), np.zeros(ncurves), 10 ** rng.uniform(np.log10(5), 2, ncurves)],
+                  axis=1)
+    offsets = np.concatenate([[0], np.cumsum(lens)])
+    t = np.concatenate([np.sort(rng.uniform(-1.0 * te, 1.0 * te, n)) for te, n in zip(cv[:, 10], lens)])
+    return offsets, t, cv
+
+
+def _masses(cv):
+    e1 = cv[:, 1] / (1 + cv[:, 1] + cv[:, 2])
+    return np.stack([e1, cv[:, 1] * e1, 1 - e1 - cv[:, 1] * e1], axis=1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_triple_light_curves(precision):
+    """Triple-lens light curves in one batched call equal the single-curve
+    mag() of each curve (the same contour kernel; every point through the
+    contour integral, as the reference's mag()).  The batched kernel forms the
+    source position on the device, the single-curve call takes it from the
+    host: the same to 1e-9 where every mass fraction is >= 1e-2; around a lens
+    of mass fraction below 1e-2 FP64 fixes the clustered roots only to ~1e-8
+    (sqrt of the rounding), so 1e-6 there.  Mixed precision there is compared
+    with the single-curve FP64 result (which takes FP64 for such lenses from
+    the start), within 1e-4."""
+    off, t, cv = draw_triple_curves(6, seed=31)
+    kw = dict(npts_limb=100, limb_darkening=True, npts_ld=40)
+    m, route, st = C.mag_lc_batched(off, t, cv, precision=precision, return_route=True, return_status=True, **kw)
+    m, route, st = m.cpu().numpy(), route.cpu().numpy(), st.cpu().numpy()
+    assert route.all() and not np.any(st & (L.ST_INVALID | L.ST_CAPACITY))
+    small = (_masses(cv) < 1e-2).any(axis=1)
+    assert small.any() and (~small).any()
+    for c in range(len(cv)):
+        s, q, q3, r3, psi, rho, u1, u0, al, t0, te = cv[c]
+        tau = (t[off[c]:off[c + 1]] - t0) / te
+        w = (u0 * np.cos(al) + tau * np.sin(al)) + 1j * (-u0 * np.sin(al) + tau * np.cos(al))
+        single = precision if (precision == "fp64" or not small[c]) else "fp64"
+        ref = C.mag(w, rho, nlenses=3, s=s, q=q, q3=q3, r3=r3, psi=psi, u1=u1, precision=single, **kw)
+        tol = 1e-4 if single != precision else (1e-6 if small[c] else 1e-9)
+        assert np.max(np.abs(m[off[c]:off[c + 1]] - ref) / ref) < tol, (c, small[c])
+
+
+def test_batched_triple_refusals_and_invalid_curves():
+    off, t, cv = draw_triple_curves(3, seed=32)
+    with pytest.raises(L.CausticsError, match="triple_routing"):
+        C.mag_lc_batched(off, t, cv, precision="fp64", npts_limb=100, triple_routing="corrected")
+    cv = cv.copy()
+    cv[1, 5] = -1.0  # rho < 0: that curve's points are not evaluated
+    m, st = C.mag_lc_batched(off, t, cv, precision="fp64", npts_limb=100, return_status=True)
+    m, st = m.cpu().numpy(), st.cpu().numpy()
+    bad = slice(off[1], off[2])
+    assert np.all(np.isnan(m[bad])) and np.all(st[bad] == L.ST_INVALID)
+    assert np.all(np.isfinite(m[off[0]:off[1]])) and np.all(np.isfinite(m[off[2]:]))
