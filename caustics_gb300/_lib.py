@@ -86,6 +86,9 @@ SIGNATURES = {
                                               ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
     "cgb_mag_lc_batched_triple": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P,
                                                  ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
+    "cgb_mag_lc_batched_triple_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, _P,
+                                                     ctypes.POINTER(EsOptions), _P, ctypes.c_size_t, _P]),
+    "cgb_mag_lc_batched_triple_vjp_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
 }
 
 _lock = threading.Lock()

@@ -385,9 +385,11 @@ def _batched_args(offsets, t, curves, triple=False):
     return off.contiguous(), tt.contiguous(), cv.contiguous()
 
 
-def _workspace(n, device, vjp=False):
-    nbytes = int(L.lib().cgb_mag_lc_batched_vjp_workspace_bytes(n) if vjp else
-                 L.lib().cgb_mag_lc_batched_workspace_bytes(n))
+def _workspace(n, device, vjp=False, triple=False):
+    lib = L.lib()
+    nbytes = int(lib.cgb_mag_lc_batched_workspace_bytes(n) if not vjp else
+                 (lib.cgb_mag_lc_batched_triple_vjp_workspace_bytes(n) if triple else
+                  lib.cgb_mag_lc_batched_vjp_workspace_bytes(n)))
     return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device), nbytes
 
 
@@ -433,23 +435,27 @@ def mag_lc_batched(offsets, t, curves, npts_limb=200, limb_darkening=False, npts
 def mag_lc_batched_vjp(offsets, t, curves, cot, npts_limb=200, limb_darkening=False, npts_ld=100, roots_itmax=2500,
                        precision="mixed", grid=0, queue_chunk=1, ld_group=1, grad_fp64_above=0.0,
                        labelling="reference", cta_threads=0, point_lanes=0):
-    """(grad [ncurves, 8], mag [npoints]): grad[c] = sum_i cot[i] d mag_i / d curves[c].
-    point_lanes is accepted for symmetry with mag_lc_batched; the adjoint's
-    per-point pass takes one thread per point."""
-    off, tt, cv = _batched_args(offsets, t, curves)
+    """(grad [ncurves, 8 or 11], mag [npoints]): grad[c] = sum_i cot[i] d mag_i /
+    d curves[c], for binary-lens curves [ncurves, 8] or triple-lens curves
+    [ncurves, 11] (the columns of mag_lc_batched).  point_lanes is accepted for
+    symmetry with mag_lc_batched; the adjoint's per-point pass takes one thread
+    per point."""
+    triple = np.ndim(curves) == 2 and np.shape(curves)[1] == 11
+    off, tt, cv = _batched_args(offsets, t, curves, triple)
     ct, _ = _to_device(cot, torch.float64)
     n = tt.numel()
     dev = tt.device
     mag_out = torch.empty(n, dtype=torch.float64, device=dev)
     route = torch.empty(n, dtype=torch.uint8, device=dev)
-    grad = torch.empty((cv.shape[0], 8), dtype=torch.float64, device=dev)
-    ws, nbytes = _workspace(n, dev, vjp=True)
+    grad = torch.empty((cv.shape[0], cv.shape[1]), dtype=torch.float64, device=dev)
+    ws, nbytes = _workspace(n, dev, vjp=True, triple=triple)
     opts = _es_options(npts_limb, limb_darkening, 0.0, npts_ld, roots_itmax, precision, grid, queue_chunk, ld_group,
                        grad_fp64_above, labelling, cta_threads=cta_threads)
+    fn = "cgb_mag_lc_batched_triple_vjp" if triple else "cgb_mag_lc_batched_vjp"
     with torch.cuda.device(dev):
-        L.check(L.lib().cgb_mag_lc_batched_vjp(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
-                                               _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
-                                               _stream()), "cgb_mag_lc_batched_vjp")
+        L.check(getattr(L.lib(), fn)(_ptr(off), _ptr(tt), _ptr(cv), cv.shape[0], n, _ptr(ct.contiguous()),
+                                     _ptr(grad), _ptr(mag_out), _ptr(route), None, opts, _ptr(ws), nbytes,
+                                     _stream()), fn)
     return grad, mag_out
 
 

@@ -353,6 +353,10 @@ size_t cgb_mag_lc_batched_vjp_workspace_bytes(int64_t npoints) {
   return cgb_mag_lc_batched_workspace_bytes(npoints) + 64 * (size_t)(npoints > 0 ? npoints : 0);
 }
 
+size_t cgb_mag_lc_batched_triple_vjp_workspace_bytes(int64_t npoints) {
+  return cgb_mag_lc_batched_workspace_bytes(npoints) + 88 * (size_t)(npoints > 0 ? npoints : 0);
+}
+
 // nl: 2 (curves: cgb_curve_params) or 3 (cgb_curve_params_triple); the
 // options are checked against a lens of that many masses (shared memory).
 static int batched_setup(const int64_t *offsets, const double *t, const void *curves, int64_t ncurves,
@@ -452,6 +456,45 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
                    "cgb_mag_lc_batched_vjp contour pass");
   if (rc) return rc;
   return cuda_status(launch_curve_grad_reduce(offsets, ncurves, P.grow, grad, s), "cgb_mag_lc_batched_vjp curve sums");
+}
+
+int cgb_mag_lc_batched_triple_vjp(const int64_t *offsets, const double *t, const cgb_curve_params_triple *curves,
+                                  int64_t ncurves, int64_t npoints, const double *cot, double *grad, double *mag,
+                                  uint8_t *route, uint32_t *status, const cgb_es_options *opts, void *workspace,
+                                  size_t workspace_bytes, void *stream) {
+  if (!grad || (npoints > 0 && (!mag || !route || !cot))) return fail(CGB_ERR_INVALID, "null buffer%s");
+  if (opts && opts->triple_routing != 0)
+    return fail(CGB_ERR_UNSUPPORTED, "batched triple-lens light curves take triple_routing 0%s");
+  if (!workspace || workspace_bytes < cgb_mag_lc_batched_triple_vjp_workspace_bytes(npoints))
+    return fail(CGB_ERR_INVALID, "workspace too small (see cgb_mag_lc_batched_triple_vjp_workspace_bytes)%s");
+  EsParams P;
+  int rc = batched_setup(offsets, t, curves, ncurves, npoints, opts, workspace, workspace_bytes, P, 3);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (npoints == 0)
+    return cuda_status(cudaMemsetAsync(grad, 0, sizeof(double) * 11 * (size_t)ncurves, s), "gradient reset");
+  {  // the adjoint kernel's shared memory for a triple lens
+    size_t smem = es_smem_bytes(P, 3, true);
+    int dev = 0, maxsmem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (maxsmem > 0 && smem + 4096 > (size_t)maxsmem)
+      return fail(CGB_ERR_UNSUPPORTED, "npts_limb too large for the triple-lens adjoint's shared memory%s");
+  }
+  rc = cuda_status(cudaMemsetAsync(workspace, 0, 16, s), "queue reset");
+  if (rc) return rc;
+  P.cot = cot;
+  P.cgrad = grad;
+  P.grow = reinterpret_cast<double *>((char *)workspace + cgb_mag_lc_batched_workspace_bytes(npoints));
+  rc = cuda_status(launch_lc_points_batched_triple(P, npoints, mag, route, status, (unsigned long long *)workspace,
+                                                   (int64_t *)((char *)workspace + 16), s, P.grow),
+                   "cgb_mag_lc_batched_triple_vjp point pass");
+  if (rc) return rc;
+  rc = cuda_status(launch_es_grad(P, nullptr, route, npoints, mag, status, opts->precision, opts->grid, s),
+                   "cgb_mag_lc_batched_triple_vjp contour pass");
+  if (rc) return rc;
+  return cuda_status(launch_curve_grad_reduce(offsets, ncurves, P.grow, grad, s, 11),
+                     "cgb_mag_lc_batched_triple_vjp curve sums");
 }
 
 int cgb_debug_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,

@@ -25,6 +25,7 @@ struct EsItem {
   double rho, u1;
   cd w0;          // source centre, shifted by x_cm
   double s, q;    // the user's lens parameters (for the adjoint's chain rule)
+  double q3, r3, psi;  // ... and the third lens's (triple lenses)
   int64_t curve;  // batched light curves: curve of the point, else -1
   double tau;     // (t - t0) / tE of the point (batched)
 };
@@ -101,7 +102,7 @@ cudaError_t launch_es_routed(const EsParams &P, const double *w0, const uint8_t 
 // cotangent-weighted gradient to P.cgrad.
 cudaError_t launch_lc_points_batched_triple(const EsParams &P, int64_t n, double *mag, uint8_t *route,
                                             uint32_t *status, unsigned long long *qcount, int64_t *qlist,
-                                            cudaStream_t stream);
+                                            cudaStream_t stream, double *grow = nullptr);
 cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, uint8_t *route, uint32_t *status,
                                      int precision, unsigned long long *qcount, int64_t *qlist, bool grad,
                                      cudaStream_t stream);
@@ -109,7 +110,7 @@ cudaError_t launch_lc_points_batched(const EsParams &P, int64_t n, double *mag, 
 // Per-curve sums of the batched adjoint's point rows: cgrad[c][k] = sum over
 // offsets[c] <= i < offsets[c+1] of grow[i][k], in a fixed order (deterministic).
 cudaError_t launch_curve_grad_reduce(const int64_t *offsets, int64_t ncurves, const double *grow, double *cgrad,
-                                     cudaStream_t stream);
+                                     cudaStream_t stream, int ncols = 8);
 
 // Gauss-Legendre nodes/weights on [-1, 1], ascending (host)
 void gauss_legendre(int n, double *x, double *w);

@@ -1275,45 +1275,70 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
     // triple (point_source.py:1807-1817): e1 = q/(1+q+q3), e2 = q e1, r3 = R e^{i psi}
     const double q = I.q, a = 0.5 * I.s, opq = 1.0 + q;
     const double ds = 0.5 * d[GK_A] + d[GK_WX] * (1.0 - q) / (2.0 * opq);
-    double dq;
+    double dq, dq3 = 0.0, dr3 = 0.0, dpsi = 0.0;
     if constexpr (NL == 2) {
       dq = -d[GK_E1] / (opq * opq) - d[GK_WX] * 2.0 * a / (opq * opq);
     } else {
-      const double den = 1.0 + q + P.q3_user, e1 = q / den;
-      const double e1_q = (1.0 + P.q3_user) / (den * den), e1_q3 = -q / (den * den);
+      const double den = 1.0 + q + I.q3, e1 = q / den;
+      const double e1_q = (1.0 + I.q3) / (den * den), e1_q3 = -q / (den * den);
       dq = d[GK_E1] * e1_q + d[GK_E2] * (e1 + q * e1_q) - d[GK_WX] * 2.0 * a / (opq * opq);
       double sp, cp;
-      sincos(P.psi_user, &sp, &cp);
-      if (P.gout) {
+      sincos(I.psi, &sp, &cp);
+      dq3 = d[GK_E1] * e1_q3 + d[GK_E2] * q * e1_q3;
+      dr3 = d[GK_R3X] * cp + d[GK_R3Y] * sp;
+      dpsi = I.r3 * (-d[GK_R3X] * sp + d[GK_R3Y] * cp);
+      if (P.gout && I.curve < 0) {
         double *gp = P.gout + pi * 9;
-        gp[6] = d[GK_E1] * e1_q3 + d[GK_E2] * q * e1_q3;     // q3
-        gp[7] = d[GK_R3X] * cp + d[GK_R3Y] * sp;              // r3
-        gp[8] = P.r3_user * (-d[GK_R3X] * sp + d[GK_R3Y] * cp);  // psi
+        gp[6] = dq3;
+        gp[7] = dr3;
+        gp[8] = dpsi;
       }
     }
     mag[pi] = mu;
-    if (NL == 2 && I.curve >= 0 && P.grow) {
-      const CurveDev cv = P.curves[I.curve];
+    if (I.curve >= 0 && P.grow) {
+      double u0, alpha, tE;
+      if constexpr (NL == 2) {
+        const CurveDev cv = P.curves[I.curve];
+        u0 = cv.u0, alpha = cv.alpha, tE = cv.tE;
+      } else {
+        const CurveDev3 cv = P.curves3[I.curve];
+        u0 = cv.u0, alpha = cv.alpha, tE = cv.tE;
+      }
       const double ct = P.cot ? P.cot[pi] : 1.0;
       double sa, ca;
-      sincos(cv.alpha, &sa, &ca);
+      sincos(alpha, &sa, &ca);
       const double tau = I.tau;
       // w = (u0 cos a + tau sin a) + i (-u0 sin a + tau cos a), tau = (t - t0)/tE
       const double du0 = d[GK_WX] * ca - d[GK_WY] * sa;
-      const double dal = d[GK_WX] * (-cv.u0 * sa + tau * ca) + d[GK_WY] * (-cv.u0 * ca - tau * sa);
-      const double dt0 = -(d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
-      const double dtE = -tau * (d[GK_WX] * sa + d[GK_WY] * ca) / cv.tE;
-      // this point's cotangent-weighted row; curve_grad_reduce_kernel sums the
-      // rows of each curve in a fixed order
-      double *gp = P.grow + pi * 8;
-      gp[0] = ct * ds;
-      gp[1] = ct * dq;
-      gp[2] = ct * d[GK_RHO];
-      gp[3] = ct * d[GK_U1];
-      gp[4] = ct * du0;
-      gp[5] = ct * dal;
-      gp[6] = ct * dt0;
-      gp[7] = ct * dtE;
+      const double dal = d[GK_WX] * (-u0 * sa + tau * ca) + d[GK_WY] * (-u0 * ca - tau * sa);
+      const double dt0 = -(d[GK_WX] * sa + d[GK_WY] * ca) / tE;
+      const double dtE = -tau * (d[GK_WX] * sa + d[GK_WY] * ca) / tE;
+      // this point's cotangent-weighted row in the curve's parameter order;
+      // curve_grad_reduce_kernel sums the rows of each curve in a fixed order
+      if constexpr (NL == 2) {
+        double *gp = P.grow + pi * 8;
+        gp[0] = ct * ds;
+        gp[1] = ct * dq;
+        gp[2] = ct * d[GK_RHO];
+        gp[3] = ct * d[GK_U1];
+        gp[4] = ct * du0;
+        gp[5] = ct * dal;
+        gp[6] = ct * dt0;
+        gp[7] = ct * dtE;
+      } else {  // (s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE)
+        double *gp = P.grow + pi * 11;
+        gp[0] = ct * ds;
+        gp[1] = ct * dq;
+        gp[2] = ct * dq3;
+        gp[3] = ct * dr3;
+        gp[4] = ct * dpsi;
+        gp[5] = ct * d[GK_RHO];
+        gp[6] = ct * d[GK_U1];
+        gp[7] = ct * du0;
+        gp[8] = ct * dal;
+        gp[9] = ct * dt0;
+        gp[10] = ct * dtE;
+      }
     } else if (P.gout) {
       double *gp = P.gout + pi * (NL == 2 ? 6 : 9);
       gp[0] = ds;
@@ -1347,6 +1372,9 @@ __device__ __forceinline__ EsItem make_item(const EsParams &P, const cd *w0s, in
     it.w0 = mk(cv.u0 * ca + tau * sa + it.L.x_cm, -cv.u0 * sa + tau * ca);
     it.s = cv.s;
     it.q = cv.q;
+    it.q3 = cv.q3;
+    it.r3 = cv.r3;
+    it.psi = cv.psi;
     it.curve = lo;
     it.tau = tau;
   } else if (P.curves) {
@@ -1365,6 +1393,7 @@ __device__ __forceinline__ EsItem make_item(const EsParams &P, const cd *w0s, in
     it.w0 = mk(cv.u0 * ca + tau * sa + it.L.x_cm, -cv.u0 * sa + tau * ca);
     it.s = cv.s;
     it.q = cv.q;
+    it.q3 = it.r3 = it.psi = 0.0;
     it.curve = lo;
     it.tau = tau;
   } else {
@@ -1375,6 +1404,9 @@ __device__ __forceinline__ EsItem make_item(const EsParams &P, const cd *w0s, in
     it.w0 = mk(w.x + P.L.x_cm, w.y);
     it.s = P.s_user;
     it.q = P.q_user;
+    it.q3 = P.q3_user;
+    it.r3 = P.r3_user;
+    it.psi = P.psi_user;
     it.curve = -1;
     it.tau = 0.0;
   }

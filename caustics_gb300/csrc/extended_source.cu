@@ -63,10 +63,11 @@ cudaError_t launch_es_grad(const EsParams &P, const double *w0, const uint8_t *r
                            uint32_t *status, int precision, int grid, cudaStream_t stream) {
   if (n == 0 && !P.qhead) return cudaSuccess;
   const cd *w = reinterpret_cast<const cd *>(w0);
-  if (!P.curves && P.L.n == 3)
+  const int nl = P.curves3 ? 3 : (P.curves ? 2 : P.L.n);
+  if (nl == 3)
     return precision == MIXED ? launch_es_variant<3, MIXED, true>(P, w, nullptr, route, n, mag, status, grid, stream)
                               : launch_es_variant<3, FP64, true>(P, w, nullptr, route, n, mag, status, grid, stream);
-  if (!P.curves && P.L.n != 2) return cudaErrorInvalidValue;
+  if (nl != 2) return cudaErrorInvalidValue;
   return precision == MIXED ? launch_es_variant<2, MIXED, true>(P, w, nullptr, route, n, mag, status, grid, stream)
                             : launch_es_variant<2, FP64, true>(P, w, nullptr, route, n, mag, status, grid, stream);
 }

@@ -31,7 +31,8 @@ __global__ void __launch_bounds__(AUX_THREADS)
     lc_points_batched_triple_kernel(const CurveDev3 *__restrict__ curves, const int64_t *__restrict__ offsets,
                                     const double *__restrict__ times, int64_t ncurves, int64_t n,
                                     double *__restrict__ mag, uint8_t *__restrict__ route,
-                                    uint32_t *__restrict__ status, unsigned long long *qcount, int64_t *qlist) {
+                                    uint32_t *__restrict__ status, unsigned long long *qcount, int64_t *qlist,
+                                    double *__restrict__ grow) {
   const int64_t i = (int64_t)blockIdx.x * AUX_THREADS + threadIdx.x;
   if (i >= n) return;
   int64_t lo = 0, hi = ncurves - 1;
@@ -44,10 +45,14 @@ __global__ void __launch_bounds__(AUX_THREADS)
                   isfinite(cv.q) && isfinite(cv.q3) && isfinite(cv.r3) && isfinite(cv.psi) && isfinite(cv.rho) &&
                   isfinite(cv.u1) && isfinite(cv.u0) && isfinite(cv.alpha) && isfinite(cv.t0) && isfinite(cv.tE) &&
                   isfinite(times[i]);
-  if (!ok) {  // not evaluated: NaN
+  if (!ok) {  // not evaluated: NaN, no gradient
     mag[i] = __longlong_as_double(0x7ff8000000000000ll);
     route[i] = 0;
     if (status) status[i] = CGB_ST_INVALID;
+    if (grow) {
+#pragma unroll
+      for (int k = 0; k < 11; ++k) grow[i * 11 + k] = 0.0;
+    }
     return;
   }
   mag[i] = 0.0;
@@ -58,16 +63,18 @@ __global__ void __launch_bounds__(AUX_THREADS)
 
 cudaError_t launch_lc_points_batched_triple(const EsParams &P, int64_t n, double *mag, uint8_t *route,
                                             uint32_t *status, unsigned long long *qcount, int64_t *qlist,
-                                            cudaStream_t stream) {
+                                            cudaStream_t stream, double *grow) {
   if (n == 0) return cudaSuccess;
   lc_points_batched_triple_kernel<<<(unsigned)((n + AUX_THREADS - 1) / AUX_THREADS), AUX_THREADS, 0, stream>>>(
-      P.curves3, P.offsets, P.times, P.ncurves, n, mag, route, status, qcount, qlist);
+      P.curves3, P.offsets, P.times, P.ncurves, n, mag, route, status, qcount, qlist, grow);
   return cudaGetLastError();
 }
 
 // cgrad[c][k] = sum of the rows grow[i][k] of curve c's points: one warp per
 // curve, each lane summing a fixed stride of points, then a fixed shuffle tree,
-// so repeated calls give identical bits.
+// so repeated calls give identical bits.  NC: the columns of a row (8
+// binary-lens curve parameters, 11 triple-lens).
+template <int NC>
 __global__ void __launch_bounds__(AUX_THREADS)
     curve_grad_reduce_kernel(const int64_t *__restrict__ offsets, int64_t ncurves, const double *__restrict__ grow,
                              double *__restrict__ cgrad) {
@@ -75,30 +82,35 @@ __global__ void __launch_bounds__(AUX_THREADS)
   const int lane = threadIdx.x & 31;
   if (c >= ncurves) return;
   const int64_t b = offsets[c], e = offsets[c + 1];
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
   for (int64_t i = b + lane; i < e; i += 32) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) acc[k] += grow[i * 8 + k];
+    for (int k = 0; k < NC; ++k) acc[k] += grow[i * NC + k];
   }
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < NC; ++k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
   }
-  if (lane < 8) {
+  if (lane < NC) {
     double v = acc[0];
 #pragma unroll
-    for (int k = 1; k < 8; ++k) v = lane == k ? acc[k] : v;
-    cgrad[c * 8 + lane] = v;
+    for (int k = 1; k < NC; ++k) v = lane == k ? acc[k] : v;
+    cgrad[c * NC + lane] = v;
   }
 }
 
 cudaError_t launch_curve_grad_reduce(const int64_t *offsets, int64_t ncurves, const double *grow, double *cgrad,
-                                     cudaStream_t stream) {
+                                     cudaStream_t stream, int ncols) {
   if (ncurves == 0) return cudaSuccess;
   constexpr int per_block = AUX_THREADS / 32;
-  curve_grad_reduce_kernel<<<(unsigned)((ncurves + per_block - 1) / per_block), AUX_THREADS, 0, stream>>>(
-      offsets, ncurves, grow, cgrad);
+  const unsigned grid = (unsigned)((ncurves + per_block - 1) / per_block);
+  if (ncols == 11)
+    curve_grad_reduce_kernel<11><<<grid, AUX_THREADS, 0, stream>>>(offsets, ncurves, grow, cgrad);
+  else
+    curve_grad_reduce_kernel<8><<<grid, AUX_THREADS, 0, stream>>>(offsets, ncurves, grow, cgrad);
   return cudaGetLastError();
 }
 

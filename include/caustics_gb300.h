@@ -295,6 +295,22 @@ int cgb_mag_lc_batched_vjp(const int64_t *offsets, const double *t, const cgb_cu
                            uint32_t *status, const cgb_es_options *opts, void *workspace, size_t workspace_bytes,
                            void *stream);
 
+/* Workspace (device bytes) of cgb_mag_lc_batched_triple_vjp: that of
+ * cgb_mag_lc_batched plus one 88-byte gradient row per point (16 + 104 npoints). */
+size_t cgb_mag_lc_batched_triple_vjp_workspace_bytes(int64_t npoints);
+
+/* Vector-Jacobian product of cgb_mag_lc_batched_triple: grad float64[ncurves,
+ * 11] = sum over the curve's points of cot[i] * d mag_i / d(s, q, q3, r3, psi,
+ * rho, u1, u0, alpha, t0, tE), the curve parameters in their own order; the
+ * reference gets the lens part from JAX autodiff through the triple parameter
+ * conversion (src/caustics/point_source.py:1807-1817).  As
+ * cgb_mag_lc_batched_vjp otherwise (every point through the contour
+ * integral; fixed-order sums). */
+int cgb_mag_lc_batched_triple_vjp(const int64_t *offsets, const double *t, const cgb_curve_params_triple *curves,
+                                  int64_t ncurves, int64_t npoints, const double *cot, double *grad, double *mag,
+                                  uint8_t *route, uint32_t *status, const cgb_es_options *opts, void *workspace,
+                                  size_t workspace_bytes, void *stream);
+
 /* Diagnostics (no counterpart in the reference): cgb_mag_extended_source that
  * also writes, per point, a record of cgb_debug_record_len(npts_limb) doubles:
  * [L, n_contours, merge flags, (start, count, parity, integral) x 13,

@@ -256,3 +256,36 @@ def test_batched_triple_refusals_and_invalid_curves():
     bad = slice(off[1], off[2])
     assert np.all(np.isnan(m[bad])) and np.all(st[bad] == L.ST_INVALID)
     assert np.all(np.isfinite(m[off[0]:off[1]])) and np.all(np.isfinite(m[off[2]:]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_triple_vjp(precision):
+    """The batched VJP of triple-lens light curves, grad [ncurves, 11] in the
+    order (s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE), against the
+    single-evaluation adjoint of each point (d mu / d(s, q, rho, u1, Re w,
+    Im w, q3, r3, psi), itself checked against central differences in
+    test_gpu_adjoint.py) chained through the trajectory on the host."""
+    off, t, cv = draw_triple_curves(4, seed=33, nmin=6, nmax=10)
+    kw = dict(npts_limb=100, limb_darkening=True, npts_ld=40)
+    cot = np.random.default_rng(4).normal(size=len(t))
+    g, m = C.mag_lc_batched_vjp(off, t, cv, cot, precision=precision, **kw)
+    g = g.cpu().numpy()
+    assert g.shape == (len(cv), 11)
+    g2, _ = C.mag_lc_batched_vjp(off, t, cv, cot, precision=precision, **kw)
+    assert np.array_equal(g, g2.cpu().numpy())  # fixed-order sums
+    for c in range(len(cv)):
+        s, q, q3, r3, psi, rho, u1, u0, al, t0, te = cv[c]
+        sl = slice(off[c], off[c + 1])
+        tau = (t[sl] - t0) / te
+        sa, ca = np.sin(al), np.cos(al)
+        w = (u0 * ca + tau * sa) + 1j * (-u0 * sa + tau * ca)
+        _, J = C.mag_extended_source_grad(w, rho, nlenses=3, s=s, q=q, q3=q3, r3=r3, psi=psi, u1=u1,
+                                          precision=precision, **kw)
+        J = np.asarray(J)
+        jx, jy = J[:, 4], J[:, 5]
+        cols = [J[:, 0], J[:, 1], J[:, 6], J[:, 7], J[:, 8], J[:, 2], J[:, 3], jx * ca - jy * sa,
+                jx * (-u0 * sa + tau * ca) + jy * (-u0 * ca - tau * sa), -(jx * sa + jy * ca) / te,
+                -tau * (jx * sa + jy * ca) / te]
+        ref = cot[sl] @ np.stack(cols, axis=1)
+        scale = np.abs(cot[sl]) @ np.abs(np.stack(cols, axis=1))
+        assert np.all(np.abs(g[c] - ref) <= 1e-6 * scale + 1e-12), (c, g[c], ref)
