@@ -117,17 +117,34 @@ __device__ int solve(const cd (&p)[DEG + 1], cd (&z)[DEG], int itmax, bool warm)
   return -1;
 }
 
-// The same iteration spread over a group of G lanes (G a power of two >= DEG,
-// G <= 32; every lane of the group calls it together): lane r owns root r.
+// The same iteration spread over a group of G lanes (DEG <= G <= 32; groups
+// tile a warp from lane 0, so a warp holds 32 / G of them; every lane of the
+// group calls it together): lane r owns root r.
 // Root j's Horner values, stopping test and z_j^2 depend on z_j alone, which
 // nothing changes before root j's own update, so all roots are evaluated at the
 // start of an iteration; then, for j in order, the terms 1/(z_j - z_i) are formed on
 // lanes i and summed in the serial order, and lane j applies its correction.
 // The arithmetic of every value is that of solve(), so the iterates are the same
 // bit for bit, at about a quarter of the sequential FP64 instructions.
+// rank of this lane in its group, the group's first lane, and its lane mask
+template <int G>
+__device__ __forceinline__ int grank() {
+  const int lane = threadIdx.x & 31;
+  return ((G & (G - 1)) == 0) ? (lane & (G - 1)) : lane % G;
+}
+template <int G>
+__device__ __forceinline__ unsigned gmask_of() {
+  const int base = (threadIdx.x & 31) - grank<G>();
+  return (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << base);
+}
 template <int G>
 __device__ __forceinline__ cd gshfl(unsigned mask, cd v, int src) {
-  return cd{__shfl_sync(mask, v.x, src, G), __shfl_sync(mask, v.y, src, G)};
+  if constexpr ((G & (G - 1)) == 0) {
+    return cd{__shfl_sync(mask, v.x, src, G), __shfl_sync(mask, v.y, src, G)};
+  } else {
+    const int s = (threadIdx.x & 31) - grank<G>() + src;
+    return cd{__shfl_sync(mask, v.x, s), __shfl_sync(mask, v.y, s)};
+  }
 }
 
 // With `target` (the DEG converged roots of the same polynomial, from a fast
@@ -137,9 +154,9 @@ __device__ __forceinline__ cd gshfl(unsigned mask, cd v, int src) {
 // so the labelling it produces is already decided.
 template <int DEG, int G>
 __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm, const cd *target = nullptr) {
-  static_assert(G >= DEG && G <= 32 && (G & (G - 1)) == 0, "group size");
-  const int lane = threadIdx.x & 31, r = lane & (G - 1);
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
+  static_assert(G >= DEG && G <= 32, "group size");
+  const int lane = threadIdx.x & 31, r = grank<G>();
+  const unsigned gmask = gmask_of<G>();
   double alpha[DEG + 1];
 #pragma unroll
   for (int i = 0; i <= DEG; ++i) alpha[i] = absc(p[i]);
@@ -220,8 +237,7 @@ __device__ int solve_group(const cd (&p)[DEG + 1], cd &zr, int itmax, bool warm,
         clear = d1 < 0.25 * d2;
         bit = 1u << best;
       }
-#pragma unroll
-      for (int o = G >> 1; o > 0; o >>= 1) bit |= __shfl_xor_sync(gmask, bit, o, G);
+      bit = __reduce_or_sync(gmask, bit);
       const bool all_clear = __all_sync(gmask, clear);
       if (all_clear && bit == all) return it + 1;
     }

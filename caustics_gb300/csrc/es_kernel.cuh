@@ -356,12 +356,11 @@ __device__ uint64_t warm_map_ref_group(const EsParams &P, const EsItem &I, doubl
   return nb;
 }
 
-template <int NL>
+template <int NL, int G = RefGroup<NL * NL + 1>::G>
 __device__ uint64_t first_point_order_group(const EsParams &P, const EsItem &I, double th, const cd *zraw,
                                             int &iters) {
-  constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G;
-  const int lane = threadIdx.x & 31, r = lane & (G - 1);
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - r));
+  constexpr int DEG = NL * NL + 1;
+  const unsigned gmask = refea::gmask_of<G>();
   double s, c;
   sincos(th, &s, &c);
   cd p[DEG + 1];
@@ -1421,25 +1420,28 @@ __device__ __forceinline__ double limb_theta(int k, int n0) {
 }
 
 // Row order of the first limb point for every item of a launch, ahead of the
-// contour kernel (which then reads perm0[item] instead of solving): one lane
-// group per item, several items per warp, so each FP64 instruction of the
-// reference's cold-start iteration serves several items.  Lane 0 of a group
-// first repeats the contour kernel's fast solve of that point (same polynomial,
-// same deterministic solver), whose roots are the raw rows to order.
-// Items are enumerated exactly as the contour kernel takes them.
+// contour kernel (which then reads perm0[item] instead of solving): one group
+// of DEG lanes per item (one lane per root), 32 / DEG groups per warp (6 of 5
+// lanes for binary lenses, 3 of 10 for triple), so each FP64 instruction of
+// the reference's cold-start iteration serves that many items.  Lane 0 of a
+// group first repeats the contour kernel's fast solve of that point (same
+// polynomial, same deterministic solver), whose roots are the raw rows to
+// order.  Items are enumerated exactly as the contour kernel takes them.
 constexpr int FO_THREADS = 128;
 template <int NL, int PREC, bool EARLY>
 __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsParams P, const cd *__restrict__ w0s,
                                                                    const int64_t *__restrict__ index,
                                                                    const uint8_t *__restrict__ route,
                                                                    int64_t npoints, uint64_t *__restrict__ perm0) {
-  constexpr int DEG = NL * NL + 1, G = RefGroup<DEG>::G, NG = FO_THREADS / G;
+  constexpr int DEG = NL * NL + 1, G = DEG, GW = 32 / G, NG = GW * (FO_THREADS / 32);
   __shared__ cd zs[NG][DEG];
-  const int g = threadIdx.x / G, r = threadIdx.x & (G - 1);
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) - r));
   // the contour kernel may start its limb sampling now; it waits for this
   // grid's completion (griddepcontrol.wait) before it reads perm0
   asm volatile("griddepcontrol.launch_dependents;");
+  const int lane = threadIdx.x & 31, gw = lane / G;
+  if (gw >= GW) return;  // the lanes past the warp's last whole group
+  const int g = (threadIdx.x >> 5) * GW + gw, r = lane - gw * G;
+  const unsigned gmask = refea::gmask_of<G>();
   const int64_t nitems = P.qhead ? *P.qcount : npoints;
   for (int64_t it = (int64_t)blockIdx.x * NG + g; it < nitems; it += (int64_t)gridDim.x * NG) {
     const int64_t pi = P.qhead ? P.qlist[it] : (index ? index[it] : it);
@@ -1456,7 +1458,7 @@ __global__ void __launch_bounds__(FO_THREADS) es_first_order_kernel(const EsPara
     }
     __syncwarp(gmask);
     int its;
-    const uint64_t o = first_point_order_group<NL>(P, I, th, zs[g], its);
+    const uint64_t o = first_point_order_group<NL, G>(P, I, th, zs[g], its);
     if (r == 0) perm0[it] = o;
     __syncwarp(gmask);
   }
