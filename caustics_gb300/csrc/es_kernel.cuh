@@ -1001,7 +1001,10 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         C u[NL];
 #pragma unroll
         for (int k = 0; k < NL; ++k) {
-          u[k] = crecip(Dj[k] + cdl);
+          if constexpr (std::is_same<R, float>::value)
+            u[k] = crecip_fast(Dj[k] + cdl);
+          else
+            u[k] = crecip(Dj[k] + cdl);
           dl = dl + cdl * u[k] * iDj[k] * (ej[k] * irho);
         }
         const C srho = C{uc.x + dl.x, uc.y + dl.y};
@@ -1019,23 +1022,43 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
             x1 = limb_gap_fp64<NL>(nl, zc, It.w0, rho, d64, isQ);
           }
         }
-        const R r = cabs(srho);
-        R B, dB;
-        if (x1 >= (R)0) {
-          const R sq = msqrt(x1);
-          B = (R)1 + sq;
-          dB = x1 > (R)0 ? -r / sq : (R)0;
+        // r = |s/rho| and its reciprocal; B(r) and dB/dr.  FP32 nodes take
+        // the approximate reciprocal and rsqrt (a few ulp, inside the FP32
+        // rounding the node values carry already) for the IEEE divisions and
+        // square roots, as the forward's nodes do
+        R r, ir, B, dB;
+        if constexpr (std::is_same<R, float>::value) {
+          const float n2 = norm2(srho);
+          ir = n2 > 0.0f ? rsqrtf(n2) : 0.0f;
+          r = n2 * ir;
+          if (x1 >= 0.0f) {
+            const float rs = x1 > 0.0f ? rsqrtf(x1) : 0.0f;
+            B = 1.0f + x1 * rs;
+            dB = -r * rs;
+          } else {
+            const float x = -x1 * ir * ir;  // 1 - 1/r^2
+            const float rs = rsqrtf(x);
+            B = 1.0f - x * rs;
+            dB = -(ir * ir * ir) * rs;
+          }
         } else {
-          const R r2 = r * r, x = -x1 / r2;  // 1 - 1/r^2
-          const R sq = msqrt(x);
-          B = (R)1 - sq;
-          dB = -(R)1 / (r2 * r * sq);
+          r = cabs(srho);
+          ir = r > (R)0 ? (R)1 / r : (R)0;
+          if (x1 >= (R)0) {
+            const R sq = msqrt(x1);
+            B = (R)1 + sq;
+            dB = x1 > (R)0 ? -r / sq : (R)0;
+          } else {
+            const R r2 = r * r, x = -x1 / r2;  // 1 - 1/r^2
+            const R sq = msqrt(x);
+            B = (R)1 - sq;
+            dB = -(R)1 / (r2 * r * sq);
+          }
         }
         const R I = c0 * (u1 * B + (R)1 - (R)2 * u1);
         const R dIdr = c0 * u1 * dB;
         const R dIdu1 = dc0 * (u1 * B + (R)1 - (R)2 * u1) + c0 * (B - (R)2);
         // unit vector of s, and d r = Re(conj(shat) ds) / rho
-        const R ir = r > (R)0 ? (R)1 / r : (R)0;
         const C sh = C{srho.x * ir, srho.y * ir};
         C lam = u[0] * u[0] * ej[0];
 #pragma unroll
