@@ -7,10 +7,13 @@
 // Algorithms (u = 2^-24): Knuth's TwoSum, TwoProd by FMA, and the double-word
 // operations of M. Joldes, J.-M. Muller, V. Popescu, "Tight and rigorous error
 // bounds for basic building blocks of double-word arithmetic", ACM TOMS 44
-// (2017): the accurate sum of two double-words (relative error <= 3u^2), the
-// product of two double-words with FMA (<= 5u^2) and of a double-word by a
-// float (<= 2u^2).  Quotient and square root take the FP32 result and one
-// Newton correction computed with those operations (relative error ~1e-13).
+// (2017): the sum of two double-words in its sloppy form (error <= ~2u^2 of
+// the operands' magnitudes, the bound the quadrature's FP64 form has in units
+// of its own rounding; the accurate form, 3u^2 of the result, costs twice the
+// instructions), the product of two double-words with FMA (<= 5u^2) and of a
+// double-word by a float (<= 2u^2).  Quotient and square root take the FP32
+// result and one Newton correction computed with those operations (relative
+// error ~1e-13).
 // Values must stay in the FP32 exponent range; the quadrature that uses them
 // does (lengths and parameters of order 1e-4 .. 1e4).
 #pragma once
@@ -44,10 +47,13 @@ CGB_HD dw dw_two_sum(float a, float b) {
   const float t = s - a;
   return dw(s, (a - (s - t)) + (b - t));
 }
+// Sum of two double-words: TwoSum of the high parts, the low parts added in
+// FP32 (the "sloppy" sum).  Its error is at most ~2u^2 (|x| + |y|): relative
+// to the operands, not the result, as FP64's own rounding of a sum is bounded
+// by u64 |x + y| only for the result of one operation, and u^2 = 2^-48.
 CGB_HD dw operator+(dw x, dw y) {
-  const dw s = dw_two_sum(x.hi, y.hi), t = dw_two_sum(x.lo, y.lo);
-  const dw v = dw_fast_two_sum(s.hi, s.lo + t.hi);
-  return dw_fast_two_sum(v.hi, t.lo + v.lo);
+  const dw s = dw_two_sum(x.hi, y.hi);
+  return dw_fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
 }
 CGB_HD dw operator-(dw x) { return dw(-x.hi, -x.lo); }
 CGB_HD dw operator-(dw x, dw y) { return x + (-y); }

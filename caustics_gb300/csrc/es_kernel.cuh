@@ -1157,7 +1157,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
                             double (*contour_acc)[MAX_CLOSED + N_CONTOURS], double (*cgr)[2],
                             double (*cgr_w)[MAX_CLOSED + N_CONTOURS][2], double (*pgr_w)[NK_MAX], double *tot_sh,
                             int64_t pi, double *mag, const float (*glf)[4][GL_MAX]) {
-  constexpr int DEG = NL * NL + 1, NK = GradDirs<NL>::NK;
+  constexpr int NK = GradDirs<NL>::NK;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     double tot = 0.0;
@@ -1197,17 +1197,31 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
           // scattered into the neighbours' position adjoints, where it would become
           // (P_ip - P_in) / 2: a difference of nearly equal quadrature values that
           // amplifies their rounding (FP32 nodes) by |P| / |dP| ~ 1e4.
-          cd tn[NK], tp[NK], ti[NK];
-          image_tangents<NL>(I, zn, tn);
-          image_tangents<NL>(I, zp, tp);
-          image_tangents<NL>(I, zc, ti);
           // Near a critical curve the tangents grow like 1/|det J| and the
           // pointwise contributions cancel in the sum; there the FP32 node values
           // (relative error ~1e-7) would be amplified, so such points run the
-          // quadrature in FP64.
+          // quadrature in FP64 (double-word under mixed precision).  Only the
+          // differences t_in - t_ip stay live across the quadrature.
           double amp2 = 0.0;
+          cd dt[NK];
+          {
+            cd t[NK];
+            image_tangents<NL>(I, zn, t);
   #pragma unroll
-          for (int k = 0; k < NK; ++k) amp2 = fmax(amp2, fmax(norm2(ti[k]), fmax(norm2(tn[k]), norm2(tp[k]))));
+            for (int k = 0; k < NK; ++k) {
+              amp2 = fmax(amp2, norm2(t[k]));
+              dt[k] = t[k];
+            }
+            image_tangents<NL>(I, zp, t);
+  #pragma unroll
+            for (int k = 0; k < NK; ++k) {
+              amp2 = fmax(amp2, norm2(t[k]));
+              dt[k] = mk(dt[k].x - t[k].x, dt[k].y - t[k].y);
+            }
+            image_tangents<NL>(I, zc, t);
+  #pragma unroll
+            for (int k = 0; k < NK; ++k) amp2 = fmax(amp2, norm2(t[k]));
+          }
           PQGrad<NK> g;
           if (PREC == MIXED && amp2 <= P.grad_amp2)
             ld_pq_grad<NL, float, cf>(P, I, zc, centroid[c], g, glf);
@@ -1219,7 +1233,7 @@ __device__ void es_backward(const EsParams &P, EsSmem<NL * NL + 1> &S, const EsI
           atomicAdd(&S.GG[i].y, pc * (wx * g.Py + wy * g.Qy));
   #pragma unroll
           for (int k = 0; k < NK; ++k)
-            acc[k] += 0.5 * pc * (pq.x * (tn[k].x - tp[k].x) + pq.y * (tn[k].y - tp[k].y));
+            acc[k] += 0.5 * pc * (pq.x * dt[k].x + pq.y * dt[k].y);
           cg1 = pc * wx * g.Pa;
           cg0 = pc * wy * g.Qa;
   #pragma unroll
