@@ -452,6 +452,39 @@ def extras_lightcurve_2000(C, dev, stream, flush):
             "mixed_vs_fp64_max_rel_err": float(((ev.mag - m64).abs() / m64).max().item()), "autotuned": ev.config}
 
 
+def extras_triple_lightcurves(C, dev, stream, flush, ncurves=64, seed=11):
+    """Triple-lens limb-darkened light curves in one batched call (every point
+    through the contour integral, as the reference's mag()): lenses drawn as
+    the triple point-source workload (s, r3 ~ U[0.5, 2], q ~ logU[1e-4, 1], q3 ~
+    logU[1e-4, 1e-1], psi ~ U[0, 2pi]), rho ~ logU[1e-3, 10^-1.5], sources and
+    trajectories as the batched workload, 200-400 points per curve; forward in
+    both precisions and the VJP w.r.t. the 11 curve parameters."""
+    import torch
+    rng = np.random.default_rng(seed)
+    n = ncurves
+    lens = rng.integers(200, 401, n)
+    cv = np.stack([rng.uniform(0.5, 2, n), 10 ** rng.uniform(-4, 0, n), 10 ** rng.uniform(-4, -1, n),
+                   rng.uniform(0.5, 2, n), rng.uniform(0, 2 * np.pi, n), 10 ** rng.uniform(-3, -1.5, n),
+                   rng.uniform(0.2, 0.8, n), rng.uniform(-0.3, 0.3, n), rng.uniform(0, 2 * np.pi, n), np.zeros(n),
+                   10 ** rng.uniform(np.log10(5), 2, n)], axis=1)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    t = np.concatenate([np.sort(rng.uniform(-te, te, m)) for te, m in zip(cv[:, 10], lens)])
+    od, td, cvd = (torch.as_tensor(x, device=dev) for x in (off, t, cv))
+    cot = torch.as_tensor(np.random.default_rng(seed).normal(size=len(t)), device=dev)
+    f32 = lambda: C.mag_lc_batched(od, td, cvd, precision="mixed", **LC)
+    f64 = lambda: C.mag_lc_batched(od, td, cvd, precision="fp64", **LC)
+    fv = lambda: C.mag_lc_batched_vjp(od, td, cvd, cot, precision="mixed", **LC)
+    m32, m64 = f32(), f64()
+    fv()
+    ms, ms64, vms = (timed(stream, f, reps=2, flush=flush) for f in (f32, f64, fv))
+    npts = len(t)
+    return {"workload": f"{n} triple-lens curves x 200-400 points (seed {seed}), npts_limb 200, npts_ld 100, LD; "
+                        "grad w.r.t. (s, q, q3, r3, psi, rho, u1, u0, alpha, t0, tE)",
+            "points": npts, "mixed_evals_per_s": npts / (ms * 1e-3), "fp64_evals_per_s": npts / (ms64 * 1e-3),
+            "vjp_evals_per_s": npts / (vms * 1e-3), "vjp_over_forward_time": vms / ms,
+            "mixed_vs_fp64_max_rel_err": float(((m32 - m64).abs() / m64.abs()).max().item())}
+
+
 def extras_triple(C, dev, stream, nsys=1000, npos=1000):
     """Triple-lens point source over the whole triple workload (seed 1: 1000
     systems s1, s2 ~ U[0.5, 2], q1 ~ logU[1e-4, 1], q2 ~ logU[1e-4, 1e-1], psi ~
@@ -623,6 +656,7 @@ def main():
                                                        * plain)
         res["binary_ld_lightcurve_2000pt"] = extras_lightcurve_2000(C, dev, stream, flush)
         res["triple_lens"] = extras_triple(C, dev, stream)
+        res["triple_lens_lightcurves"] = extras_triple_lightcurves(C, dev, stream, flush)
     if pool is not None:
         rate, n = cpu_rate(pool, cores, per_core=48, seed=99)
         pool.close()

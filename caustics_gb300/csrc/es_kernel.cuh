@@ -938,6 +938,11 @@ template <int NL, typename R, typename C>
 __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQGrad<GradDirs<NL>::NK> &g,
                            const float (*glf)[4][GL_MAX]) {
   constexpr int NK = GradDirs<NL>::NK, NLD = GradDirs<NL>::NLENS;
+  // The direct parameter terms Ck (rho, u1, w0, lens) sum node values that no
+  // image tangent multiplies later; the double-word nodes, which exist for the
+  // terms the tangents amplify (the value and the position derivatives), keep
+  // them in FP32.
+  using CkT = typename std::conditional<std::is_same<R, dw>::value, float, R>::type;
   // shifted lens equation around the contour point
   const double rho = It.rho, inv_rho = 1.0 / rho;
   // D_j = conj(zc) - conj(r_j) and 1 / D_j, which lens_eq(zc) = zc - sum_j
@@ -979,7 +984,8 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
       const R lo_r = (R)(lo - b), hi_r = (R)(hi - b);
       const R hw = (R)0.5 * (hi_r - lo_r), mid = (R)0.5 * (hi_r + lo_r);
       const int n = half ? P.n2 : P.n1;
-      R A = 0, Bl = 0, Bh = 0, Cf = 0, Ck[NK];
+      R A = 0, Bl = 0, Bh = 0, Cf = 0;
+      CkT Ck[NK];
 #pragma unroll
       for (int k = 0; k < NK; ++k) Ck[k] = 0;
       for (int j = 0; j < n; ++j) {
@@ -1063,8 +1069,6 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         C lam = u[0] * u[0] * ej[0];
 #pragma unroll
         for (int k = 1; k < NL; ++k) lam = lam + u[k] * u[k] * ej[k];
-        C dsl[NLD];
-        lens_shifts<NL, R, C>(u, ej, dsl);
         // d s / d x' = 1 + lam ; d s / d y' = i (1 - lam)
         const R drx = (sh.x * ((R)1 + lam.x) + sh.y * lam.y) * irho;
         const R dry = (sh.x * lam.y + sh.y * ((R)1 - lam.x)) * irho;
@@ -1075,17 +1079,38 @@ __device__ void ld_pq_grad(const EsParams &P, const EsItem &It, cd zc, cd z0, PQ
         Bl += w * Iy * (R)0.5 * ((R)1 - t);
         Bh += w * Iy * (R)0.5 * ((R)1 + t);
         Cf += w * dIdr * dr_fixed;
-        Ck[GK_RHO] += w * dIdr * (-r * irho);
-        Ck[GK_U1] += w * dIdu1;
-        Ck[GK_WX] += w * dIdr * (-sh.x * irho);
-        Ck[GK_WY] += w * dIdr * (-sh.y * irho);
+        if constexpr (std::is_same<R, dw>::value) {
+          // the direct parameter terms from the high words, in FP32
+          const float wd = w.hi * dIdr.hi, irf = irho.hi, shx = sh.x.hi, shy = sh.y.hi;
+          cf uf[NL], dslf[NLD];
+          float ejf[NL];
 #pragma unroll
-        for (int m = 0; m < NLD; ++m) Ck[GK_A + m] += w * dIdr * ((sh.x * dsl[m].x + sh.y * dsl[m].y) * irho);
+          for (int k = 0; k < NL; ++k) {
+            uf[k] = cf{u[k].x.hi, u[k].y.hi};
+            ejf[k] = ej[k].hi;
+          }
+          lens_shifts<NL, float, cf>(uf, ejf, dslf);
+          Ck[GK_RHO] += wd * (-r.hi * irf);
+          Ck[GK_U1] += w.hi * dIdu1.hi;
+          Ck[GK_WX] += wd * (-shx * irf);
+          Ck[GK_WY] += wd * (-shy * irf);
+#pragma unroll
+          for (int m = 0; m < NLD; ++m) Ck[GK_A + m] += wd * ((shx * dslf[m].x + shy * dslf[m].y) * irf);
+        } else {
+          C dsl[NLD];
+          lens_shifts<NL, R, C>(u, ej, dsl);
+          Ck[GK_RHO] += w * dIdr * (-r * irho);
+          Ck[GK_U1] += w * dIdu1;
+          Ck[GK_WX] += w * dIdr * (-sh.x * irho);
+          Ck[GK_WY] += w * dIdr * (-sh.y * irho);
+#pragma unroll
+          for (int m = 0; m < NLD; ++m) Ck[GK_A + m] += w * dIdr * ((sh.x * dsl[m].x + sh.y * dsl[m].y) * irho);
+        }
       }
       val += hw * A;
       fixed += hw * Cf;
 #pragma unroll
-      for (int k = 0; k < NK; ++k) kk[k] += hw * Ck[k];
+      for (int k = 0; k < NK; ++k) kk[k] += hw * (R)Ck[k];
       dlo[half] = (R)-0.5 * A + hw * Bl;
       dhi[half] = (R)0.5 * A + hw * Bh;
     }
