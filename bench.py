@@ -75,10 +75,10 @@ FP64_PIPE_BUSY_NCU = 0.571
 # the same for es_kernel<2, MIXED, GRAD> (the VJP's contour kernel), one
 # launch over 2000 contour evaluations of the gradient workload
 NCU_EVALS_VJP = 2000
-DRAM_BYTES_PER_EVAL_VJP = 13.68e6 / NCU_EVALS_VJP
+DRAM_BYTES_PER_EVAL_VJP = 13.89e6 / NCU_EVALS_VJP
 FP64_FLOP_PER_EVAL_VJP = 3.3826e9 / NCU_EVALS_VJP
-FP32_FLOP_PER_EVAL_VJP = 6.2463e10 / NCU_EVALS_VJP
-FP64_PIPE_BUSY_NCU_VJP = 0.668
+FP32_FLOP_PER_EVAL_VJP = 6.1482e10 / NCU_EVALS_VJP
+FP64_PIPE_BUSY_NCU_VJP = 0.671
 
 
 def draw_batched(ncurves_total, seed, nmin, nmax, take):
