@@ -138,6 +138,34 @@ __device__ __forceinline__ void lens_poly(const Lens &L, cd w, cd (&p)[NL * NL +
     for (int k = 0; k <= NL; ++k) p[i + k] = p[i + k] - L.D[k] * S[i];
 }
 
+// Coefficient m (0..5) of lens_poly<2>(L, w): the terms of p[m] only, added in
+// the order lens_poly adds them, so that six lanes, one per coefficient, give
+// lens_poly's values with a dependent chain about half as long.
+__device__ __forceinline__ cd lens_poly2_coef(const Lens &L, cd w, int m) {
+  const cd wb = conj(w);
+  cd G[2][3];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const cd c = wb - conj(L.r[j]);
+#pragma unroll
+    for (int k = 0; k <= 2; ++k) G[j][k] = (k < 2) ? cfma(c, L.D[k], L.N[k]) : c * L.D[k];
+  }
+  auto prod = [&](int n) {  // prod_j G_j, coefficient n
+    cd a = mk(0, 0);
+#pragma unroll
+    for (int i = 0; i <= 2; ++i)
+      if (n - i >= 0 && n - i <= 2) a = cfma(G[0][i], G[1][n - i], a);
+    return a;
+  };
+  cd v = mk(0, 0);
+  if (m >= 1) v = v + prod(m - 1);
+  if (m <= 4) v = v - w * prod(m);
+#pragma unroll
+  for (int i = 0; i <= 2; ++i)
+    if (m - i >= 0 && m - i <= 2) v = v - L.D[m - i] * (G[1][i] * L.eps[0] + G[0][i] * L.eps[1]);
+  return v;
+}
+
 // w = z - sum_j eps_j / (conj(z) - conj(r_j))   (point_source.py:1536-1556)
 template <int NL>
 __device__ __forceinline__ cd lens_eq(const Lens &L, cd z) {
