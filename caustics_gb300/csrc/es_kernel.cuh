@@ -2198,16 +2198,16 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
       uint16_t *NBP = reinterpret_cast<uint16_t *>(NBV + nbs);
       long long *MGV = reinterpret_cast<long long *>(rtmp + (((size_t)nbs * 10 + 15) & ~(size_t)15));  // merged
       uint16_t *MGP = reinterpret_cast<uint16_t *>(MGV + (ngap + nsel));
-      for (int j = tid; j < nbs; j += ES_THREADS) {
-        if (j < nsel) {
-          const int k = NEWK[j], sl = S.ORD[k], sr = S.ORD[k + 1], m = Lcur + j;
-          NBV[2 * j] = __double_as_longlong(interval_len<DEG>(S, sl, m));
-          NBP[2 * j] = (uint16_t)(k + j);
-          NBV[2 * j + 1] = __double_as_longlong(interval_len<DEG>(S, m, sr));
-          NBP[2 * j + 1] = (uint16_t)(k + j + 1);
-        } else if (j >= nb) {
-          NBV[j] = -1ll;
-          NBP[j] = 0;
+      // one lane per new interval (e = 2 j: left of new point j, 2 j + 1: right)
+      for (int e = tid; e < nbs; e += ES_THREADS) {
+        if (e < nb) {
+          const int j = e >> 1, side = e & 1, k = NEWK[j], m = Lcur + j;
+          const double len = side ? interval_len<DEG>(S, m, S.ORD[k + 1]) : interval_len<DEG>(S, S.ORD[k], m);
+          NBV[e] = __double_as_longlong(len);
+          NBP[e] = (uint16_t)(k + j + side);
+        } else {
+          NBV[e] = -1ll;
+          NBP[e] = 0;
         }
       }
       for (int r = nsel + tid; r < ngap; r += ES_THREADS) SLP[r] = (uint16_t)(SLP[r] + S.SCAN[SLP[r]]);
