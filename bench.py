@@ -68,10 +68,10 @@ def f_es(L, G):
 # FP32 arithmetic (dadd + dmul + 2 dfma, fadd + fmul + 2 ffma thread
 # instructions).
 NCU_EVALS = 2764
-DRAM_BYTES_PER_EVAL = 5.667e6 / NCU_EVALS
-FP64_FLOP_PER_EVAL = 1.1378e9 / NCU_EVALS
+DRAM_BYTES_PER_EVAL = 6.547e6 / NCU_EVALS
+FP64_FLOP_PER_EVAL = 1.2939e9 / NCU_EVALS
 FP32_FLOP_PER_EVAL = 2.3732e10 / NCU_EVALS
-FP64_PIPE_BUSY_NCU = 0.571
+FP64_PIPE_BUSY_NCU = 0.581
 # the same for es_kernel<2, MIXED, GRAD> (the VJP's contour kernel), one
 # launch over 2000 contour evaluations of the gradient workload
 NCU_EVALS_VJP = 2000

@@ -79,7 +79,7 @@ __host__ __device__ inline Lens make_lens(int nlenses, double s, double q, doubl
 
 // Polynomial coefficients, low -> high, for source position w (already shifted).
 template <int NL>
-__device__ __forceinline__ void lens_poly(const Lens &L, cd w, cd (&p)[NL * NL + 2]) {
+CGB_HD void lens_poly(const Lens &L, cd w, cd (&p)[NL * NL + 2]) {
   constexpr int DEG = NL * NL + 1;
   cd wb = conj(w);
   cd G[NL][NL + 1];
@@ -141,7 +141,7 @@ __device__ __forceinline__ void lens_poly(const Lens &L, cd w, cd (&p)[NL * NL +
 // Coefficient m (0..5) of lens_poly<2>(L, w): the terms of p[m] only, added in
 // the order lens_poly adds them, so that six lanes, one per coefficient, give
 // lens_poly's values with a dependent chain about half as long.
-__device__ __forceinline__ cd lens_poly2_coef(const Lens &L, cd w, int m) {
+CGB_HD cd lens_poly2_coef(const Lens &L, cd w, int m) {
   const cd wb = conj(w);
   cd G[2][3];
 #pragma unroll
