@@ -1855,48 +1855,49 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
         // first two warps; each lane forms its point's source position and one
         // coefficient (lens_poly2_coef), a chain half as long as the whole
         // polynomial on one lane
-        if constexpr (NL == 2)
-        for (int idx = tid; idx < nsel * (DEG + 1); idx += ES_THREADS) {
-          const int j = idx / (DEG + 1), m = idx - j * (DEG + 1);
-          const int k = NEWK[j], slot = Lcur + j;
-          const int sl = S.ORD[k], sr = S.ORD[k + 1];
-          const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
-          double sn, cs;
-          sincos(th, &sn, &cs);
-          const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
-          pco[(size_t)j * (DEG + 2) + m] = lens_poly2_coef(I.L, w, m);
-          if (m < DEG)  // warm start from the left neighbour's rows with the fixed jitter
-            S.Z[(size_t)slot * DEG + m] =
-                S.Z[(size_t)sl * DEG + m] + mk(1e-6 * ((m & 1) ? 0.5 : -0.5), 1e-6 * ((m & 2) ? 0.5 : -0.5));
-          if (m == 0) {
+        if constexpr (NL == 2) {
+          for (int idx = tid; idx < nsel * (DEG + 1); idx += ES_THREADS) {
+            const int j = idx / (DEG + 1), m = idx - j * (DEG + 1);
+            const int k = NEWK[j], slot = Lcur + j;
+            const int sl = S.ORD[k], sr = S.ORD[k + 1];
+            const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
+            pco[(size_t)j * (DEG + 2) + m] = lens_poly2_coef(I.L, w, m);
+            if (m < DEG)  // warm start from the left neighbour's rows with the fixed jitter
+              S.Z[(size_t)slot * DEG + m] =
+                  S.Z[(size_t)sl * DEG + m] + mk(1e-6 * ((m & 1) ? 0.5 : -0.5), 1e-6 * ((m & 2) ? 0.5 : -0.5));
+            if (m == 0) {
+              S.TH[slot] = th;
+              psl[j] = sl;
+              pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
+            }
+          }
+        } else {
+          // one thread per new point, dense over the first warps: FP64 work
+          // spread over every warp costs each warp the whole instruction stream
+          for (int j = tid; j < nsel; j += ES_THREADS) {
+            const int k = NEWK[j], slot = Lcur + j;
+            const int sl = S.ORD[k], sr = S.ORD[k + 1];
+            const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
             S.TH[slot] = th;
             psl[j] = sl;
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
+            cd p[DEG + 1];
+            lens_poly<NL>(I.L, w, p);
+#pragma unroll
+            for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
             pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
+            // warm start from the left neighbour's rows with the fixed jitter
+            // (extended_source.py:79-98, 128-129)
+#pragma unroll
+            for (int i = 0; i < DEG; ++i)
+              S.Z[(size_t)slot * DEG + i] =
+                  S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
           }
-        }
-        // one thread per new point, dense over the first warps: FP64 work
-        // spread over every warp costs each warp the whole instruction stream
-        else
-        for (int j = tid; j < nsel; j += ES_THREADS) {
-          const int k = NEWK[j], slot = Lcur + j;
-          const int sl = S.ORD[k], sr = S.ORD[k + 1];
-          const double th = 0.5 * (S.TH[sl] + S.TH[sr]);
-          S.TH[slot] = th;
-          psl[j] = sl;
-          double sn, cs;
-          sincos(th, &sn, &cs);
-          const cd w = mk(__dadd_rn(__dmul_rn(I.rho, cs), I.w0.x), __dadd_rn(__dmul_rn(I.rho, sn), I.w0.y));
-          cd p[DEG + 1];
-          lens_poly<NL>(I.L, w, p);
-#pragma unroll
-          for (int i = 0; i <= DEG; ++i) pco[(size_t)j * (DEG + 2) + i] = p[i];
-          pco[(size_t)j * (DEG + 2) + DEG + 1] = w;
-          // warm start from the left neighbour's rows with the fixed jitter
-          // (extended_source.py:79-98, 128-129)
-#pragma unroll
-          for (int i = 0; i < DEG; ++i)
-            S.Z[(size_t)slot * DEG + i] =
-                S.Z[(size_t)sl * DEG + i] + mk(1e-6 * ((i & 1) ? 0.5 : -0.5), 1e-6 * ((i & 2) ? 0.5 : -0.5));
         }
         __syncthreads();
         // The FP32 stage on a lane group per new point, one lane per root,
