@@ -73,6 +73,13 @@ SIGNATURES = {
                                _P, _P]),
     "cgb_mag_extended_source_grad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
                                                     ctypes.POINTER(EsOptions), _P, _P]),
+    "cgb_mag_extended_source_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+    "cgb_mag_extended_source_ws": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
+                                                  ctypes.POINTER(EsOptions), _P, _P, ctypes.c_size_t, _P]),
+    "cgb_mag_extended_source_grad_ws": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
+                                                       ctypes.POINTER(EsOptions), _P, _P, ctypes.c_size_t, _P]),
+    "cgb_mag_ws": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, LensParams, ctypes.POINTER(EsOptions),
+                                  _P, _P, ctypes.c_size_t, _P]),
     "cgb_debug_extended_source": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, LensParams,
                                                  ctypes.POINTER(EsOptions), _P, _P, _P]),
     "cgb_debug_record_len": (ctypes.c_int64, [ctypes.c_int32]),

@@ -307,6 +307,12 @@ def _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, 
                        int(cta_threads), int(point_lanes))
 
 
+def _es_workspace(n, device):
+    """Scratch of the single-evaluation *_ws entry points: one first-limb-point
+    row order (8 bytes) per source position."""
+    return torch.empty(max(n, 1), dtype=torch.int64, device=device)
+
+
 def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False, u1=0.0, npts_ld=100,
                         roots_itmax=2500, roots_compensated=False, precision=None, return_status=False, grid=0,
                         labelling="reference", **params):
@@ -322,9 +328,11 @@ def mag_extended_source(w0, rho, nlenses=2, npts_limb=150, limb_darkening=False,
     mag = torch.empty(n, dtype=torch.float64, device=wf.device)
     st = torch.zeros(n, dtype=torch.int32, device=wf.device)
     opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling)
+    ws = _es_workspace(n, wf.device)
     with torch.cuda.device(wf.device):
-        L.check(L.lib().cgb_mag_extended_source(_ptr(wf), _ptr(mag), n, float(rho), L.lens_params(nlenses, params),
-                                                opts, _ptr(st), _stream()), "cgb_mag_extended_source")
+        L.check(L.lib().cgb_mag_extended_source_ws(_ptr(wf), _ptr(mag), n, float(rho), L.lens_params(nlenses, params),
+                                                   opts, _ptr(st), _ptr(ws), ws.numel() * 8, _stream()),
+                "cgb_mag_extended_source_ws")
     if scalar:
         m = float(mag[0].item())
         return (m, int(st[0].item())) if return_status else m
@@ -352,9 +360,10 @@ def mag(w_points, rho, nlenses=2, npts_limb=200, limb_darkening=False, u1=0.0, n
     st = torch.zeros(n, dtype=torch.int32, device=wf.device)
     opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid, labelling=labelling,
                        triple_routing=triple_routing)
+    ws = _es_workspace(n, wf.device)
     with torch.cuda.device(wf.device):
-        L.check(L.lib().cgb_mag(_ptr(wf), _ptr(out), _ptr(route), n, float(rho), L.lens_params(nlenses, params), opts,
-                                _ptr(st), _stream()), "cgb_mag")
+        L.check(L.lib().cgb_mag_ws(_ptr(wf), _ptr(out), _ptr(route), n, float(rho), L.lens_params(nlenses, params),
+                                   opts, _ptr(st), _ptr(ws), ws.numel() * 8, _stream()), "cgb_mag_ws")
     res = [_out(out.reshape(shape), was_np)]
     if return_route:
         res.append(_out(route.reshape(shape).bool(), was_np))
@@ -493,10 +502,12 @@ def mag_extended_source_grad(w0, rho, nlenses=2, npts_limb=150, limb_darkening=F
     g = torch.empty((n, 6 if nlenses == 2 else 9), dtype=torch.float64, device=wf.device)
     opts = _es_options(npts_limb, limb_darkening, u1, npts_ld, roots_itmax, precision, grid,
                        grad_fp64_above=grad_fp64_above, labelling=labelling)
+    ws = _es_workspace(n, wf.device)
     with torch.cuda.device(wf.device):
-        L.check(L.lib().cgb_mag_extended_source_grad(_ptr(wf), _ptr(mag_out), _ptr(g), n, float(rho),
-                                                     L.lens_params(nlenses, params), opts, None, _stream()),
-                "cgb_mag_extended_source_grad")
+        L.check(L.lib().cgb_mag_extended_source_grad_ws(_ptr(wf), _ptr(mag_out), _ptr(g), n, float(rho),
+                                                        L.lens_params(nlenses, params), opts, None, _ptr(ws),
+                                                        ws.numel() * 8, _stream()),
+                "cgb_mag_extended_source_grad_ws")
     return _out(mag_out, was_np), _out(g, was_np)
 
 

@@ -300,13 +300,29 @@ int cgb_mag_point_source(const double *w, double *mag, double *images, uint32_t 
                      "cgb_mag_point_source launch");
 }
 
-int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
-                            const cgb_es_options *opts, uint32_t *status, void *stream) {
+// Workspace of the single-evaluation entry points (the *_ws forms): one
+// first-limb-point row order (8 bytes, 8-byte aligned) per source position, so
+// that es_first_order_kernel orders every item's first limb point ahead of the
+// contour kernel, as in the batched path.
+size_t cgb_mag_extended_source_workspace_bytes(int64_t n) { return n > 0 ? 8 * (size_t)n : 0; }
+
+static int es_workspace(EsParams &P, int64_t n, void *ws, size_t ws_bytes) {
+  if (n <= 0) return 0;
+  if (!ws || ws_bytes < cgb_mag_extended_source_workspace_bytes(n) || ((uintptr_t)ws & 7u))
+    return fail(CGB_ERR_INVALID, "workspace: 8 bytes per source position, 8-byte aligned%s");
+  P.perm0 = reinterpret_cast<const uint64_t *>(ws);
+  return 0;
+}
+
+static int mag_extended_source_impl(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                                    const cgb_es_options *opts, uint32_t *status, void *ws, size_t ws_bytes,
+                                    void *stream) {
   if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
   if (n > 0 && (!w0 || !mag)) return fail(CGB_ERR_INVALID, "null buffer%s");
   EsParams P;
   int rc = make_es_params(lens, rho, opts, P);
   if (rc) return rc;
+  if (ws && (rc = es_workspace(P, n, ws, ws_bytes))) return rc;
   int grid = opts->grid > 0 ? opts->grid : (int)((n < 8 * sm_count()) ? n : 8 * sm_count());
   if (grid < 1) grid = 1;
   return cuda_status(launch_es(P, w0, nullptr, n, mag, status, solver_precision(lens, opts->precision), grid,
@@ -314,12 +330,26 @@ int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho
                      "cgb_mag_extended_source launch");
 }
 
-int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, int64_t n, double rho,
-                                 cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status, void *stream) {
+int cgb_mag_extended_source(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                            const cgb_es_options *opts, uint32_t *status, void *stream) {
+  return mag_extended_source_impl(w0, mag, n, rho, lens, opts, status, nullptr, 0, stream);
+}
+
+int cgb_mag_extended_source_ws(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                               const cgb_es_options *opts, uint32_t *status, void *workspace,
+                               size_t workspace_bytes, void *stream) {
+  if (n > 0 && !workspace) return fail(CGB_ERR_INVALID, "null workspace%s");
+  return mag_extended_source_impl(w0, mag, n, rho, lens, opts, status, workspace, workspace_bytes, stream);
+}
+
+static int mag_extended_source_grad_impl(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                         cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status,
+                                         void *ws, size_t ws_bytes, void *stream) {
   if (n < 0 || (n > 0 && (!w0 || !mag || !grad))) return fail(CGB_ERR_INVALID, "invalid buffers%s");
   EsParams P;
   int rc = make_es_params(lens, rho, opts, P);
   if (rc) return rc;
+  if (ws && (rc = es_workspace(P, n, ws, ws_bytes))) return rc;
   if (lens.nlenses == 3) {  // the adjoint's accumulators may need shared memory beyond the forward's
     int dev = 0, maxsmem = 0;
     cudaGetDevice(&dev);
@@ -337,6 +367,19 @@ int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, in
   if (grid < 1) grid = 1;
   return cuda_status(launch_es_grad(P, w0, nullptr, n, mag, status, opts->precision, grid, (cudaStream_t)stream),
                      "cgb_mag_extended_source_grad launch");
+}
+
+int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                 cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status, void *stream) {
+  return mag_extended_source_grad_impl(w0, mag, grad, n, rho, lens, opts, status, nullptr, 0, stream);
+}
+
+int cgb_mag_extended_source_grad_ws(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                    cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status,
+                                    void *workspace, size_t workspace_bytes, void *stream) {
+  if (n > 0 && !workspace) return fail(CGB_ERR_INVALID, "null workspace%s");
+  return mag_extended_source_grad_impl(w0, mag, grad, n, rho, lens, opts, status, workspace, workspace_bytes,
+                                       stream);
 }
 
 // Workspace of the batched entry points: a 16-byte queue header, one queue
@@ -515,13 +558,14 @@ int64_t cgb_debug_record_len(int32_t npts_limb) {
   return ES_DBG_STRIDE(n0 + 10 * (n0 / 10));
 }
 
-int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
-            const cgb_es_options *opts, uint32_t *status, void *stream) {
+static int mag_impl(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+                    const cgb_es_options *opts, uint32_t *status, void *ws, size_t ws_bytes, void *stream) {
   if (n < 0) return fail(CGB_ERR_INVALID, "n must be >= 0%s");
   if (n > 0 && (!w || !mag || !route)) return fail(CGB_ERR_INVALID, "null buffer%s");
   EsParams P;
   int rc = make_es_params(lens, rho, opts, P);
   if (rc) return rc;
+  if (ws && (rc = es_workspace(P, n, ws, ws_bytes))) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const int prec = solver_precision(lens, opts->precision);
   const int prec_ps = point_source_precision(lens, prec) == CGB_PREC_MIXED ? MIXED : FP64;
@@ -535,6 +579,17 @@ int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho,
   if (grid < 1) grid = 1;
   return cuda_status(launch_es_routed(P, w, route, n, mag, status, prec, grid, s),
                      "cgb_mag contour pass launch");
+}
+
+int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+            const cgb_es_options *opts, uint32_t *status, void *stream) {
+  return mag_impl(w, mag, route, n, rho, lens, opts, status, nullptr, 0, stream);
+}
+
+int cgb_mag_ws(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+               const cgb_es_options *opts, uint32_t *status, void *workspace, size_t workspace_bytes, void *stream) {
+  if (n > 0 && !workspace) return fail(CGB_ERR_INVALID, "null workspace%s");
+  return mag_impl(w, mag, route, n, rho, lens, opts, status, workspace, workspace_bytes, stream);
 }
 
 // ---- batched light curves without any allocation ----

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define CGB_ABI_VERSION 5
+#define CGB_ABI_VERSION 6
 
 /* launch status */
 #define CGB_OK 0
@@ -225,6 +225,27 @@ int cgb_mag_extended_source_grad(const double *w0, double *mag, double *grad, in
  * integral was used.  Replaces mag (src/caustics/lightcurve.py:99-254). */
 int cgb_mag(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
             const cgb_es_options *opts, uint32_t *status, void *stream);
+
+/* Workspace (device bytes) of the *_ws forms below for n source positions:
+ * one 8-byte first-limb-point row order per position (8 n), 8-byte aligned. */
+size_t cgb_mag_extended_source_workspace_bytes(int64_t n);
+
+/* cgb_mag_extended_source, cgb_mag_extended_source_grad and cgb_mag with a
+ * caller-owned device workspace of at least
+ * cgb_mag_extended_source_workspace_bytes(n) bytes: a separate kernel orders
+ * the first limb point of every evaluation ahead of the contour kernel (as the
+ * batched entry points do), instead of one lane group per CTA doing it inside
+ * the contour kernel.  Same results bit for bit, faster; the workspace is
+ * scratch for the duration of the call (stream-ordered).  CGB_ERR_INVALID for
+ * a null, short or misaligned workspace when n > 0. */
+int cgb_mag_extended_source_ws(const double *w0, double *mag, int64_t n, double rho, cgb_lens_params lens,
+                               const cgb_es_options *opts, uint32_t *status, void *workspace,
+                               size_t workspace_bytes, void *stream);
+int cgb_mag_extended_source_grad_ws(const double *w0, double *mag, double *grad, int64_t n, double rho,
+                                    cgb_lens_params lens, const cgb_es_options *opts, uint32_t *status,
+                                    void *workspace, size_t workspace_bytes, void *stream);
+int cgb_mag_ws(const double *w, double *mag, uint8_t *route, int64_t n, double rho, cgb_lens_params lens,
+               const cgb_es_options *opts, uint32_t *status, void *workspace, size_t workspace_bytes, void *stream);
 
 /* Workspace (device bytes) the batched entry points use for npoints points:
  * a 16-byte work-queue header, one 8-byte queue slot per point, then one

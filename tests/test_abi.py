@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 def test_host_entry_points(lib):
     from caustics_gb300 import _lib as L
-    assert lib.cgb_abi_version() == 5
+    assert lib.cgb_abi_version() == 6
     for n in (2, 7, 50, 100):
         x = np.zeros(n)
         w = np.zeros(n)
