@@ -9,9 +9,9 @@ shape functions) and differentiable through the hand-written adjoints
 
   caustics::ea_solve ................. cgb_ea_solve (backward: cgb_ea_roots_vjp)
   caustics::mag_point_source ......... cgb_mag_point_source
-  caustics::mag_extended_source ...... cgb_mag_extended_source
-                                       (backward: cgb_mag_extended_source_grad)
-  caustics::mag ...................... cgb_mag
+  caustics::mag_extended_source ...... cgb_mag_extended_source_ws
+                                       (backward: cgb_mag_extended_source_grad_ws)
+  caustics::mag ...................... cgb_mag_ws
   caustics::mag_lc_batched ........... cgb_mag_lc_batched (backward: cgb_mag_lc_batched_vjp)
   caustics::mag_lc_batched_vjp ....... cgb_mag_lc_batched_vjp
 
