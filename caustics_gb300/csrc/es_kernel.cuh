@@ -2023,13 +2023,18 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
             cd *zrow = S.Z + (size_t)slot * DEG;
             uint32_t f = lg < DEG ? rflag[j * DEG + lg] : 1u;
             auto distinct = [&]() {  // no two roots closer than 1e-7 of the largest modulus
-              double scale = 0.0;
+              // the largest |z|^2 by a shuffle tree (lane r: root r), then the
+              // DEG (DEG - 1) / 2 pairs dealt evenly over the group's lanes:
+              // the same exact comparisons on a shorter FP64 chain per lane
+              double scale = lg < DEG ? norm2(zrow[lg]) : 0.0;
 #pragma unroll
-              for (int q = 0; q < DEG; ++q) scale = fmax(scale, norm2(zrow[q]));
+              for (int o = 1; o < FG; o <<= 1) scale = fmax(scale, __shfl_xor_sync(gmask, scale, o, FG));
               bool sep = true;
-              if (lg < DEG)
-                for (int q = lg + 1; q < DEG; ++q)
-                  if (norm2(zrow[lg] - zrow[q]) < 1e-14 * scale) sep = false;
+              for (int pr = lg; pr < DEG * (DEG - 1) / 2; pr += FG) {
+                int a = 0, rem = pr;
+                while (rem >= DEG - 1 - a) rem -= DEG - 1 - (a++);
+                if (norm2(zrow[a] - zrow[a + 1 + rem]) < 1e-14 * scale) sep = false;
+              }
               return __all_sync(gmask, sep);
             };
             bool ok = pok[j] != 0 && __all_sync(gmask, (f & 1u) != 0);
