@@ -2108,14 +2108,17 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
             // step_map on the group: lane r finds row r's nearest and second
             // nearest new root; clear when every row's nearest is nearer than
             // half its second nearest and no two rows share one
+            // (squared distances are >= +0, so their bit patterns order as
+            // unsigned integers, any NaN above +inf: the comparisons run on
+            // the integer pipe)
             int best = 0;
             bool clear = true;
             if (lg < DEG) {
               const cd ar = S.Z[(size_t)sl * DEG + lg];
-              double d1 = INFINITY, d2 = INFINITY;
+              unsigned long long d1 = (unsigned long long)__double_as_longlong(INFINITY), d2 = d1;
 #pragma unroll
               for (int q = 0; q < DEG; ++q) {
-                const double d = norm2(zrow[q] - ar);
+                const unsigned long long d = (unsigned long long)__double_as_longlong(norm2(zrow[q] - ar));
                 if (d < d1) {
                   d2 = d1;
                   d1 = d;
@@ -2124,7 +2127,7 @@ __global__ void __launch_bounds__(ES_MAX_THREADS, NL == 2 ? 2 : 1) es_kernel(con
                   d2 = d;
                 }
               }
-              clear = d1 < 0.25 * d2;
+              clear = __longlong_as_double((long long)d1) < 0.25 * __longlong_as_double((long long)d2);
             }
             uint32_t bits = lg < DEG ? (1u << best) : 0u;
 #pragma unroll
