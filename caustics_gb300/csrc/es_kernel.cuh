@@ -295,11 +295,13 @@ __device__ uint64_t step_map(const cd *a, const cd *b, bool &ambiguous) {
   uint64_t res = 0;
   uint32_t used = 0;
   ambiguous = false;
+  // squared distances are >= +0: compared as their bit patterns (unsigned,
+  // any NaN above +inf) on the integer pipe
   for (int i = 0; i < DEG; ++i) {
-    double d1 = INFINITY, d2 = INFINITY;
+    unsigned long long d1 = (unsigned long long)__double_as_longlong(INFINITY), d2 = d1;
     int best = 0;
     for (int j = 0; j < DEG; ++j) {
-      double d = norm2(b[j] - a[i]);
+      const unsigned long long d = (unsigned long long)__double_as_longlong(norm2(b[j] - a[i]));
       if (d < d1) {
         d2 = d1;
         d1 = d;
@@ -308,7 +310,8 @@ __device__ uint64_t step_map(const cd *a, const cd *b, bool &ambiguous) {
         d2 = d;
       }
     }
-    if (!(d1 < 0.25 * d2) || ((used >> best) & 1u)) ambiguous = true;
+    if (!(__longlong_as_double((long long)d1) < 0.25 * __longlong_as_double((long long)d2)) || ((used >> best) & 1u))
+      ambiguous = true;
     used |= 1u << best;
     res = perm_set(res, i, best);
   }
